@@ -1,0 +1,47 @@
+/*
+ * oracle.h - C entry points of the CPU oracle (liboracle.so).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker the CUDA library is compared with.
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
+ * It consumes the same rt_scene_desc as the library (include/radiantium.h).
+ */
+#ifndef RT_ORACLE_H
+#define RT_ORACLE_H
+#include "../include/radiantium.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* builds the restated Scene; NULL on error (message in err) */
+void* or_scene_create(const rt_scene_desc* scene, char* err, int errlen);
+void or_scene_destroy(void* s);
+
+/* Scene.Intersect / Scene.Intersect(ray) over a batch (threads <= 0: all cores) */
+int or_trace_closest(void* s, const rt_ray* rays, int64_t n, rt_hit* hits, int threads);
+int or_trace_any(void* s, const rt_ray* rays, int64_t n, uint8_t* occluded, int threads);
+
+/* BlockBasedRenderer over the crop; out_rgb in ColorBuffer layout of the crop.
+ * stats (nullable) receives the summed counters. */
+int or_render(void* s, const rt_render_params* p, float* out_rgb, int threads, rt_stats* stats);
+
+/* per-sample radiance (no averaging): out[((x*h + y) * spp + k) * 3 + c] */
+int or_render_samples(void* s, const rt_render_params* p, float* out, int threads);
+
+/* PerspectiveCamera.SampleRay for n screen positions (2 floats each) */
+int or_camera_rays(void* s, const float* screen_pos, int64_t n, rt_ray* out);
+
+/* flattened reference BVH: which = -1 top level, k >= 0 instanced prototype k.
+ * bounds: 6 floats per node, idx: PrimitivesIndex/SecondChildIndex,
+ * count: PrimitiveCount, axis: Axis, prim_order: primitive id per ordered slot.
+ * Call with NULL arrays to query sizes. */
+int or_bvh(void* s, int which, int64_t* node_count, int64_t* prim_count,
+           float* bounds, int32_t* idx, int32_t* count, int32_t* axis, int32_t* prim_order);
+
+/* deterministic math and RNG known-answer hooks */
+int or_detmath(int fn, const float* a, const float* b, float* out, int64_t n);
+int or_philox(uint64_t seed, uint32_t x, uint32_t y, uint32_t s, int count, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

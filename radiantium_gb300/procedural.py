@@ -1,0 +1,238 @@
+"""Seeded procedural scenes for the benchmark workloads.
+
+The reference ships no benchmark scenes; these generators build, from a seed,
+the workloads its headline metric is quoted on:
+
+* :func:`cornell_box`  - plain path integrator, procedural Cornell box in a unit
+  cube: 5 wall quads (10 tris), 2 rotated boxes (24 tris), a ceiling quad light
+  (radiance 15), Lambertian albedos 0.73 / 0.65 / 0.12, 256x256, 64 spp, depth 5.
+* :func:`instanced_spheres` - 64 instances of a ~200k-triangle displaced sphere,
+  GGX conductors (alpha ~ U[0.05, 0.5]) and rough dielectrics (IOR 1.5), lit
+  by a 1024x512 HDR environment of 8 Gaussian lobes, 1024x1024, 256 spp, depth 8.
+* :func:`volume_sphere` - vol_path: ~500k-triangle displaced sphere bounding a
+  homogeneous medium (sigma_a 0.05, sigma_s 2.0, HG g 0.7) over a diffuse
+  ground with one quad light, 512x512, 512 spp, depth 32.
+
+Every scene is a :class:`~radiantium_gb300.scene.SceneDesc` built through the
+same tables the reference's RendererBuilder fills (meshes per entity,
+materials with texture parameters, instanced prototypes, infinite light).
+Only IEEE-exact float operations (and float64 noise rounded to float32) are
+used so the meshes are identical on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import native as N
+from .scene import (Camera, Group, Mat4, Material, Medium, Mesh, RenderSettings, SceneDesc, Texture,
+                    transform_points)
+
+# copper conductor eta / k in RGB (rough_metal default metal_type "Cu")
+CU_ETA = (0.1999899, 0.9220823, 1.0998751)
+CU_K = (3.9046354, 2.4476316, 2.1376500)
+
+
+# ------------------------------------------------------------------ geometry ----
+def quad(p0, p1, p2, p3) -> Mesh:
+    """Two triangles (p0,p1,p2), (p0,p2,p3); normal = normalize(cross(p1-p0, p2-p0))."""
+    pos = np.array([p0, p1, p2, p3], dtype=np.float32)
+    return Mesh(pos, np.array([[0, 1, 2], [0, 2, 3]], dtype=np.int32))
+
+
+def box_mesh(center, size, angle_deg) -> Mesh:
+    """Axis-aligned box of `size`, rotated about +y by `angle_deg`, outward normals."""
+    sx, sy, sz = (s * 0.5 for s in size)
+    corners = np.array([[x, y, z] for x in (-sx, sx) for y in (-sy, sy) for z in (-sz, sz)], dtype=np.float64)
+    a = math.radians(angle_deg)
+    c, s = math.cos(a), math.sin(a)
+    rot = np.array([[c, 0, -s], [0, 1, 0], [s, 0, c]])
+    pts = (corners @ rot.T + np.asarray(center)).astype(np.float32)
+    # faces as corner index quads (x,y,z bits: x*4 + y*2 + z)
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    idx = []
+    for q in faces:
+        idx += [[q[0], q[1], q[2]], [q[0], q[2], q[3]]]
+    idx = np.array(idx, dtype=np.int32)
+    idx = _orient_outward(pts, idx, pts.mean(axis=0))
+    return Mesh(pts, idx)
+
+
+def _orient_outward(pos, idx, center):
+    a, b, c = pos[idx[:, 0]].astype(np.float64), pos[idx[:, 1]].astype(np.float64), pos[idx[:, 2]].astype(np.float64)
+    n = np.cross(b - a, c - a)
+    out = ((a + b + c) / 3.0) - np.asarray(center, dtype=np.float64)
+    flip = (n * out).sum(axis=1) < 0
+    idx = idx.copy()
+    idx[flip] = idx[flip][:, [0, 2, 1]]
+    return idx
+
+
+def _hash3(ix, iy, iz, seed):
+    """Integer lattice hash (xorshift-multiply mix) -> float64 in [-1, 1)."""
+    h = (ix.astype(np.uint64) * np.uint64(0x8DA6B343) ^ iy.astype(np.uint64) * np.uint64(0xD8163841)
+         ^ iz.astype(np.uint64) * np.uint64(0xCB1AB31F) ^ np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15))
+    h = h & np.uint64(0xFFFFFFFFFFFFFFFF)
+    h ^= h >> np.uint64(33)
+    h *= np.uint64(0xFF51AFD7ED558CCD)
+    h ^= h >> np.uint64(33)
+    h *= np.uint64(0xC4CEB9FE1A85EC53)
+    h ^= h >> np.uint64(33)
+    return (h >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+
+
+def value_noise(p: np.ndarray, seed: int, octaves: int = 3) -> np.ndarray:
+    """Seeded 3-D value noise (smoothstep-interpolated lattice values), fBm sum in [-1, 1]."""
+    total = np.zeros(p.shape[0])
+    amp, norm, freq = 1.0, 0.0, 1.0
+    with np.errstate(over="ignore"):
+        for o in range(octaves):
+            q = p * freq
+            i0 = np.floor(q)
+            f = q - i0
+            w = f * f * (3.0 - 2.0 * f)
+            i0 = i0.astype(np.int64) + 1024
+            acc = np.zeros(p.shape[0])
+            for dx in (0, 1):
+                for dy in (0, 1):
+                    for dz in (0, 1):
+                        val = _hash3(i0[:, 0] + dx, i0[:, 1] + dy, i0[:, 2] + dz, seed * 131 + o)
+                        wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                        wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                        wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                        acc += val * wx * wy * wz
+            total += amp * acc
+            norm += amp
+            amp *= 0.5
+            freq *= 2.0
+    return total / norm
+
+
+def displaced_sphere(n: int, seed: int, amplitude: float = 0.06, frequency: float = 3.0) -> Mesh:
+    """Cube-sphere with n x n quads per face (12 n^2 triangles), radius 1 + amplitude * noise,
+    counter-clockwise seen from outside.  Seam vertices are computed from identical
+    cube coordinates, so shared edges have bit-identical end points."""
+    t = np.tan((np.arange(n + 1) / n * 2.0 - 1.0) * (math.pi / 4.0))  # equal-angle warp
+    u, v = np.meshgrid(t, t, indexing="ij")
+    u, v = u.reshape(-1), v.reshape(-1)
+    one = np.ones_like(u)
+    faces = [np.stack([one, u, v], 1), np.stack([-one, v, u], 1), np.stack([v, one, u], 1),
+             np.stack([u, -one, v], 1), np.stack([u, v, one], 1), np.stack([v, u, -one], 1)]
+    pos, idx = [], []
+    g = np.arange((n + 1) * (n + 1)).reshape(n + 1, n + 1)
+    a, b, c, d = g[:-1, :-1].reshape(-1), g[1:, :-1].reshape(-1), g[1:, 1:].reshape(-1), g[:-1, 1:].reshape(-1)
+    quad_idx = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)])
+    for k, f in enumerate(faces):
+        pos.append(f)
+        idx.append(quad_idx + k * (n + 1) * (n + 1))
+    cube = np.concatenate(pos)
+    idx = np.concatenate(idx).astype(np.int32)
+    dirs = cube / np.sqrt((cube * cube).sum(1, keepdims=True))
+    r = 1.0 + amplitude * value_noise(dirs * frequency, seed)
+    p = (dirs * r[:, None]).astype(np.float32)
+    idx = _orient_outward(p, idx, np.zeros(3))
+    return Mesh(p, idx)
+
+
+def gaussian_lobe_env(width: int, height: int, seed: int, lobes: int = 8) -> Texture:
+    """Lat-long HDR radiance map: sky base + `lobes` Gaussian lobes on the sphere.
+    Texel (x, y) covers phi = 2 pi (x+0.5)/w, theta = pi (y+0.5)/h with the
+    direction convention of InfiniteAreaLight.Le (phi = atan2(x, -z), theta = acos y)."""
+    rng = np.random.default_rng(seed)
+    phi = (np.arange(width) + 0.5) / width * 2 * math.pi
+    theta = (np.arange(height) + 0.5) / height * math.pi
+    th, ph = np.meshgrid(theta, phi, indexing="ij")  # (h, w)
+    d = np.stack([np.sin(th) * np.sin(ph), np.cos(th), -np.sin(th) * np.cos(ph)], -1)
+    img = np.zeros((height, width, 3)) + np.array([0.03, 0.04, 0.06]) * (0.5 + 0.5 * d[..., 1:2].clip(0, 1))
+    for k in range(lobes):
+        z = rng.uniform(-0.2, 1.0)
+        a = rng.uniform(0, 2 * math.pi)
+        axis = np.array([math.sqrt(1 - z * z) * math.cos(a), z, math.sqrt(1 - z * z) * math.sin(a)])
+        sharp = rng.uniform(8.0, 400.0) if k else 2000.0
+        color = rng.uniform(0.2, 1.0, 3) * (rng.uniform(2.0, 20.0) if k else 200.0)
+        img += color * np.exp((d @ axis - 1.0) * sharp)[..., None]
+    return Texture.from_image_hw3(img.astype(np.float32))
+
+
+# -------------------------------------------------------------------- scenes ----
+def cornell_box(width=256, height=256):
+    """Procedural Cornell box in the unit cube [0,1]^3, open towards +z."""
+    s = SceneDesc(camera=Camera.look_at(width, height, 40.0, (0.5, 0.5, 2.3), (0.5, 0.5, 0.0)), name="cornell")
+    white = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.73, 0.73, 0.73))))
+    red = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.65, 0.05, 0.05))))
+    green = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.12, 0.45, 0.15))))
+    lightmat = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.5, 0.5, 0.5))))
+    # inward-facing walls: floor, ceiling, back, left (red), right (green)
+    walls = [
+        (quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)), white),
+        (quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)), white),
+        (quad((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)), white),
+        (quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), red),
+        (quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), green),
+    ]
+    for mesh, m in walls:
+        s.groups.append(Group(N.GROUP_MESH, s.add_mesh(mesh), material=m))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(box_mesh((0.66, 0.15, 0.62), (0.3, 0.3, 0.3), -17.0)), material=white))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(box_mesh((0.34, 0.3, 0.36), (0.3, 0.6, 0.3), 17.0)), material=white))
+    light = quad((0.4, 0.999, 0.4), (0.6, 0.999, 0.4), (0.6, 0.999, 0.6), (0.4, 0.999, 0.6))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(light), material=lightmat, emissive=True, le=(15.0, 15.0, 15.0)))
+    settings = RenderSettings(N.INTEGRATOR_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=5, min_depth=3,
+                              rr_threshold=0.99, spp=64, seed=1)
+    return s, settings
+
+
+def instanced_spheres(width=1024, height=1024, sphere_n=129, grid=8, env_w=1024, env_h=512, seed=7):
+    """64 instances of one displaced sphere (12 * 129^2 = 199,692 triangles)."""
+    rng = np.random.default_rng(seed)
+    s = SceneDesc(camera=Camera.look_at(width, height, 40.0, (0.0, 13.0, 21.0), (0.0, 0.0, 0.0)), name="instanced")
+    proto = s.add_mesh(displaced_sphere(sphere_n, seed))
+    s.blas.append([Group(N.GROUP_MESH, proto)])
+    zero = s.add_const(0.0)
+    one = s.add_const(1.0)
+    spacing = 2.6
+    for gi in range(grid):
+        for gj in range(grid):
+            alpha = float(rng.uniform(0.05, 0.5))
+            rough = s.add_const(math.sqrt(alpha))
+            if (gi + gj) % 2 == 0:
+                m = s.add_material(Material(N.MAT_ROUGH_METAL, N.DIST_GGX, tex_roughness=rough, tex_anisotropic=zero,
+                                            eta=CU_ETA, k=CU_K))
+            else:
+                m = s.add_material(Material(N.MAT_ROUGH_GLASS, N.DIST_GGX, tex_r=one, tex_t=one, tex_roughness=rough,
+                                            tex_anisotropic=zero, eta_a=1.0, eta_b=1.5))
+            scale = float(rng.uniform(1.0, 1.25))
+            ang = float(rng.uniform(0, 2 * math.pi))
+            pos = ((gi - (grid - 1) / 2) * spacing, scale, (gj - (grid - 1) / 2) * spacing)
+            m2w = Mat4.scale((scale, scale, scale)) * Mat4.from_axis_angle((0, 1, 0), ang) * Mat4.translation(pos)
+            s.groups.append(Group(N.GROUP_INSTANCE, 0, material=m, model_to_world=m2w))
+    env = s.add_texture(gaussian_lobe_env(env_w, env_h, seed))
+    s.groups.append(Group(N.GROUP_INFINITE_LIGHT, env))
+    settings = RenderSettings(N.INTEGRATOR_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=8, min_depth=3,
+                              rr_threshold=0.99, spp=256, seed=1)
+    return s, settings
+
+
+def volume_sphere(width=512, height=512, sphere_n=204, seed=11):
+    """vol_path: displaced sphere (12 * 204^2 = 499,392 triangles) with no material
+    bounding a homogeneous medium, diffuse ground, one quad light."""
+    s = SceneDesc(camera=Camera.look_at(width, height, 45.0, (0.0, 1.6, 5.0), (0.0, 1.0, 0.0)), name="volume")
+    ground = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.5, 0.5, 0.5))))
+    lightmat = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.5, 0.5, 0.5))))
+    med = s.add_medium(Medium((0.05, 0.05, 0.05), (2.0, 2.0, 2.0), g=0.7, scale=1.0))
+    sph = displaced_sphere(sphere_n, seed, amplitude=0.08).transformed(Mat4.translation((0.0, 1.1, 0.0)))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(sph), material=-1, medium_inside=med, medium_outside=-1))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(quad((-10, 0, -10), (-10, 0, 10), (10, 0, 10), (10, 0, -10))),
+                          material=ground))
+    light = quad((-0.75, 4.0, -0.75), (0.75, 4.0, -0.75), (0.75, 4.0, 0.75), (-0.75, 4.0, 0.75))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(light), material=lightmat, emissive=True, le=(20.0, 20.0, 20.0)))
+    settings = RenderSettings(N.INTEGRATOR_VOL_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=32, min_depth=3,
+                              rr_threshold=0.99, spp=512, seed=1)
+    return s, settings
+
+
+WORKLOADS = {
+    "cornell": cornell_box,
+    "instanced": instanced_spheres,
+    "volume": volume_sphere,
+}
