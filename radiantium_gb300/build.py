@@ -1,0 +1,67 @@
+"""Builds libradiantium_gb300.so in-tree for sm_103a.
+
+Three translation units compiled in parallel and linked with nvcc:
+  rt_kernels.cu  device code: --fmad=false keeps every multiply and add
+                 separately rounded (the reference's arithmetic), IEEE
+                 division and square root are nvcc's defaults;
+  rt_host.cpp, rt_bvh.cpp  host runtime and BVH builder, -ffp-contract=off
+                 for the same reason.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUT_DIR, "libradiantium_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def _cuda_home():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return c
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(nvcc))
+    raise RuntimeError("nvcc not found")
+
+
+def build(verbose: bool = False, extra_nvcc=()) -> str:
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(OUT_DIR, exist_ok=True)
+    objs = {
+        "rt_kernels.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_kernels.cu")],
+        "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                      f"-I{cuda}/include", "-c", os.path.join(CSRC, "rt_host.cpp")],
+        "rt_bvh.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                     "-c", os.path.join(CSRC, "rt_bvh.cpp")],
+    }
+    procs = []
+    for obj, cmd in objs.items():
+        full = cmd + ["-o", os.path.join(OUT_DIR, obj)]
+        if verbose:
+            print(" ".join(full))
+        procs.append((obj, subprocess.Popen(full, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    failed = []
+    for obj, p in procs:
+        out, _ = p.communicate()
+        if out and (verbose or p.returncode):
+            sys.stdout.write(out)
+        if p.returncode:
+            failed.append(obj)
+    if failed:
+        raise RuntimeError(f"radiantium_gb300 build failed: {failed}")
+    link = [nvcc, ARCH, "-shared", "-o", LIB] + [os.path.join(OUT_DIR, o) for o in objs] + ["-lpthread"]
+    subprocess.run(link, check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

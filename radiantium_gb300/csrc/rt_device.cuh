@@ -1,0 +1,630 @@
+/*
+ * rt_device.cuh - device code of the GB300 path tracer: math, RNG, textures,
+ * BVH traversal, BxDFs, lights, media and the scene services the integrators
+ * call.
+ *
+ * Every expression keeps the operand order of the reference C# (cited per
+ * function) and the file is compiled with --fmad=false, IEEE division and
+ * square root, so a path computes the same bits as the reference's arithmetic
+ * restated on the CPU.  Transcendentals come from rt_detmath.h.
+ */
+#ifndef RT_DEVICE_CUH
+#define RT_DEVICE_CUH
+
+#include <stdint.h>
+#include "rt_types.h"
+#include "../../include/radiantium.h"
+#include "../../include/rt_detmath.h"
+
+#define DF __device__ __forceinline__
+
+namespace rtd {
+
+constexpr float kPI = 3.14159265f;
+constexpr float kEps = 1.401298464324817e-45f;   /* float.Epsilon */
+constexpr float kFMax = 3.40282347e+38f;         /* float.MaxValue */
+
+DF bool isnanf_(float x) { return x != x; }
+DF bool isinff_(float x) { return (__float_as_uint(x) & 0x7fffffffu) == 0x7f800000u; }
+DF bool isneg_(float x) { return (__float_as_uint(x) >> 31) != 0; }
+/* System.Math.Max / Min (float), NaN-propagating, +0 > -0 */
+DF float nmax(float a, float b) {
+    if (a != b) { if (!isnanf_(a)) return b < a ? a : b; return a; }
+    return isneg_(b) ? a : b;
+}
+DF float nmin(float a, float b) {
+    if (a != b) { if (!isnanf_(a)) return a < b ? a : b; return a; }
+    return isneg_(a) ? a : b;
+}
+DF float nclamp(float v, float lo, float hi) { if (v < lo) return lo; if (v > hi) return hi; return v; }
+DF int nclampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+/* (int)float as the .NET x64 JIT converts: truncation, NaN / overflow -> int.MinValue */
+DF int nf2i(float f) {
+    if (isnanf_(f) || f >= 2147483648.0f || f < -2147483648.0f) return (int)0x80000000;
+    return __float2int_rz(f);
+}
+DF float Sqrt(float x) { return __fsqrt_rn(x); }
+DF float Abs(float x) { return fabsf(x); }
+DF float Sqr(float v) { return v * v; }
+DF float MulSign(float a1, float a2) { return a1 * rt_dm_copysign(1.0f, a2); }
+DF float SafeSqrt(float a) { return Sqrt(nmax(a, 0.0f)); }
+
+struct V2 { float x, y; };
+struct V3 { float x, y, z; };
+DF V2 v2(float x, float y) { V2 r; r.x = x; r.y = y; return r; }
+DF V3 v3(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+DF V3 v3s(float s) { return v3(s, s, s); }
+DF V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+DF V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+DF V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+DF V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+DF V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+DF V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+DF V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+DF V2 operator+(V2 a, V2 b) { return v2(a.x + b.x, a.y + b.y); }
+DF V2 operator*(float s, V2 a) { return v2(s * a.x, s * a.y); }
+DF float Dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DF float AbsDot(V3 a, V3 b) { return Abs(Dot(a, b)); }
+DF V3 Cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+DF float LengthSq(V3 a) { return Dot(a, a); }
+DF float Length(V3 a) { return Sqrt(LengthSq(a)); }
+DF V3 Normalize(V3 a) { float l = Length(a); return a / l; }
+DF float Distance(V3 a, V3 b) { return Length(a - b); }
+DF V3 Reflect(V3 v, V3 n) { float d = Dot(v, n); return v - ((2.0f * d) * n); }
+DF float Get(V3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+DF V3 f4xyz(float4 f) { return v3(f.x, f.y, f.z); }
+
+/* Matrix rows: m[0..2] row 1, m[3..5] row 2, m[6..8] row 3, m[9..11] translation */
+DF V3 Xf12(V3 p, const float* m) {
+    return v3(p.x * m[0] + p.y * m[3] + p.z * m[6] + m[9],
+              p.x * m[1] + p.y * m[4] + p.z * m[7] + m[10],
+              p.x * m[2] + p.y * m[5] + p.z * m[8] + m[11]);
+}
+DF V3 XfN12(V3 v, const float* m) {
+    return v3(v.x * m[0] + v.y * m[3] + v.z * m[6],
+              v.x * m[1] + v.y * m[4] + v.z * m[7],
+              v.x * m[2] + v.y * m[5] + v.z * m[8]);
+}
+/* full Matrix4x4 (16 floats, M11..M44) used by the camera */
+DF V3 Xf16(V3 p, const float* m) {
+    return v3(p.x * m[0] + p.y * m[4] + p.z * m[8] + m[12],
+              p.x * m[1] + p.y * m[5] + p.z * m[9] + m[13],
+              p.x * m[2] + p.y * m[6] + p.z * m[10] + m[14]);
+}
+DF V3 XfN16(V3 v, const float* m) {
+    return v3(v.x * m[0] + v.y * m[4] + v.z * m[8],
+              v.x * m[1] + v.y * m[5] + v.z * m[9],
+              v.x * m[2] + v.y * m[6] + v.z * m[10]);
+}
+
+struct C3 { float r, g, b; };
+DF C3 c3(float r, float g, float b) { C3 c; c.r = r; c.g = g; c.b = b; return c; }
+DF C3 c3s(float v) { return c3(v, v, v); }
+DF C3 operator+(C3 a, C3 b) { return c3(a.r + b.r, a.g + b.g, a.b + b.b); }
+DF C3 operator-(C3 a, C3 b) { return c3(a.r - b.r, a.g - b.g, a.b - b.b); }
+DF C3 operator*(C3 a, C3 b) { return c3(a.r * b.r, a.g * b.g, a.b * b.b); }
+DF C3 operator/(C3 a, C3 b) { return c3(a.r / b.r, a.g / b.g, a.b / b.b); }
+DF C3 operator+(C3 a, float s) { return c3(a.r + s, a.g + s, a.b + s); }
+DF C3 operator-(C3 a, float s) { return c3(a.r - s, a.g - s, a.b - s); }
+DF C3 operator*(C3 a, float s) { return c3(a.r * s, a.g * s, a.b * s); }
+DF C3 operator/(C3 a, float s) { return c3(a.r / s, a.g / s, a.b / s); }
+DF C3 operator*(float s, C3 a) { return c3(s * a.r, s * a.g, s * a.b); }
+DF C3 operator-(float s, C3 a) { return c3(s - a.r, s - a.g, s - a.b); }
+DF bool IsBlack(C3 a) { return a.r == 0.0f && a.g == 0.0f && a.b == 0.0f; }
+DF bool Same(C3 a, C3 b) { return a.r == b.r && a.g == b.g && a.b == b.b; }
+DF bool IsValid(C3 c) {
+    if (c.r < 0 || isinff_(c.r) || isnanf_(c.r)) return false;
+    if (c.g < 0 || isinff_(c.g) || isnanf_(c.g)) return false;
+    if (c.b < 0 || isinff_(c.b) || isnanf_(c.b)) return false;
+    return true;
+}
+DF C3 CAbs(C3 c) { return c3(Abs(c.r), Abs(c.g), Abs(c.b)); }
+DF float MaxElement(C3 c) { return nmax(nmax(c.r, c.g), c.b); }
+DF float Luminance(C3 c) { return c.r * 0.212671f + c.g * 0.715160f + c.b * 0.072169f; }
+DF float CGet(C3 c, int i) { return i == 0 ? c.r : (i == 1 ? c.g : c.b); }
+
+/* Ray3F (Radiantium.Core/Ray3F.cs) */
+struct Ray { V3 O, D; float MinT, MaxT; V3 InvD; };
+DF Ray mkray(V3 o, V3 d, float minT = kEps, float maxT = kFMax) {
+    Ray r; r.O = o; r.D = d; r.MinT = minT; r.MaxT = maxT;
+    r.InvD = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    return r;
+}
+DF V3 At(const Ray& r, float t) { return r.O + t * r.D; }
+/* Ray3F.Transform */
+DF Ray XfRay(const Ray& ray, const float* m) {
+    V3 o = Xf12(ray.O, m);
+    V3 d = Normalize(XfN12(ray.D, m));
+    V3 mx = Xf12(At(ray, ray.MaxT), m);
+    float maxT = Distance(o, mx);
+    return mkray(o, d, ray.MinT, maxT);
+}
+
+/* Coordinate (Coordinate.cs:14-34, Duff et al. 2017) */
+struct Frame { V3 X, Y, Z; };
+DF Frame mkframe(V3 n) {
+    float sign = rt_dm_copysign(1.0f, n.z);
+    float a = -1 / (sign + n.z);
+    float b = n.x * n.y * a;
+    Frame f;
+    f.X = v3(MulSign(Sqr(n.x) * a, n.z) + 1.0f, MulSign(b, n.z), MulSign(n.x, -n.z));
+    f.Y = v3(b, sign + Sqr(n.y) * a, -n.y);
+    f.Z = n;
+    return f;
+}
+DF V3 ToLocal(const Frame& f, V3 v) { return v3(Dot(v, f.X), Dot(v, f.Y), Dot(v, f.Z)); }
+DF V3 ToWorld(const Frame& f, V3 v) { return f.X * v.x + f.Y * v.y + f.Z * v.z; }
+DF float CosTheta(V3 v) { return v.z; }
+DF float AbsCosTheta(V3 v) { return Abs(v.z); }
+DF float Cos2Theta(V3 v) { return Sqr(v.z); }
+DF float Sin2Theta(V3 v) { return v.x * v.x + Sqr(v.y); }
+DF float TanTheta(V3 v) { return SafeSqrt(-v.z * v.z + 1.0f) / v.z; }
+DF float Tan2Theta(V3 v) { return nmax(-v.z * v.z + 1.0f, 0.0f) / Sqr(v.z); }
+DF float Cos2Phi(V3 v) { float s2 = Sin2Theta(v); return Abs(s2) <= 4.0f * kEps ? 1.0f : nclamp(Sqr(v.x) / s2, -1.0f, 1.0f); }
+DF float Sin2Phi(V3 v) { float s2 = Sin2Theta(v); return Abs(s2) <= 4.0f * kEps ? 0.0f : nclamp(Sqr(v.y) / s2, -1.0f, 1.0f); }
+DF bool SameHemisphere(V3 a, V3 b) { return a.z * b.z > 0; }
+DF V3 Faceforward(V3 v, V3 w) { return (Dot(v, w) < 0.0f) ? -v : v; }
+/* MathExt.Refract */
+DF bool Refract(V3 wi, V3 n, float eta, V3* wt) {
+    float cosThetaI = Dot(n, wi);
+    float sin2ThetaI = nmax(0, 1 - cosThetaI * cosThetaI);
+    float sin2ThetaT = eta * eta * sin2ThetaI;
+    if (sin2ThetaT >= 1) { *wt = v3s(0); return false; }
+    float cosThetaT = Sqrt(1 - sin2ThetaT);
+    *wt = Normalize(eta * -wi + (eta * cosThetaI - cosThetaT) * n);
+    return true;
+}
+DF V3 SphDir(float sinTheta, float cosTheta, float phi) {
+    float sinPhi = rt_sinf(phi), cosPhi = rt_cosf(phi);
+    return v3(sinTheta * cosPhi, sinTheta * sinPhi, cosTheta);
+}
+
+/* ---- Philox4x32-10 stream (stands in for System.Random) ------------------- */
+struct Rng {
+    uint32_t k0, k1, c0, c1, c2, n;
+    uint32_t buf[4];
+};
+DF void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t* out) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+DF void rng_init(Rng& r, uint64_t seed, uint32_t x, uint32_t y, uint32_t s) {
+    r.k0 = (uint32_t)seed; r.k1 = (uint32_t)(seed >> 32); r.c0 = x; r.c1 = y; r.c2 = s; r.n = 0;
+}
+DF uint32_t next_u32(Rng& r) {
+    if ((r.n & 3u) == 0) philox(r.c0, r.c1, r.c2, r.n >> 2, r.k0, r.k1, r.buf);
+    uint32_t v;
+    switch (r.n & 3u) { case 0: v = r.buf[0]; break; case 1: v = r.buf[1]; break; case 2: v = r.buf[2]; break; default: v = r.buf[3]; }
+    r.n++;
+    return v;
+}
+DF float NextFloat(Rng& r) { return (float)(next_u32(r) >> 8) * (1.0f / 16777216.0f); }
+DF int NextInt(Rng& r, int n) { return (int)(((uint64_t)next_u32(r) * (uint64_t)(uint32_t)n) >> 32); }
+DF V2 NextVec2(Rng& r) { float a = NextFloat(r); float b = NextFloat(r); return v2(a, b); }
+
+/* Probability.cs warps */
+DF V3 SquareToCosineHemisphere(V2 s) {
+    float radius = Sqrt(s.x);
+    float angle = s.y * kPI * 2;
+    float x = radius * rt_cosf(angle), y = radius * rt_sinf(angle);
+    return v3(x, y, Sqrt(1 - x * x - y * y));
+}
+DF V3 SquareToUniformSphere(V2 s) {
+    float phi = s.x * kPI * 2;
+    float theta = rt_acosf(1 - 2 * s.y);
+    float sinTheta = rt_sinf(theta), cosTheta = rt_cosf(theta);
+    float sinPhi = rt_sinf(phi), cosPhi = rt_cosf(phi);
+    return v3(sinTheta * cosPhi, sinTheta * sinPhi, cosTheta);
+}
+/* PathUtility.PowerHeuristic (double) */
+DF float PowerHeuristic(float fPdf, float gPdf) {
+    double f = (double)(1.0f * fPdf), g = (double)(1.0f * gPdf);
+    return (float)((f * f) / (f * f + g * g));
+}
+
+/* ---- textures (TextureSampler.cs:28-72) ------------------------------------ */
+DF C3 TexRead(const RtSceneView* S, const RtTexture& t, int x, int y) {
+    x = nclampi(x, 0, t.width - 1); y = nclampi(y, 0, t.height - 1);
+    const float* p = S->texels + t.offset + ((int64_t)x * t.height + y) * 3;
+    return c3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+DF float Wrapper(float a, int mode) {
+    if (mode == RT_WRAP_CLAMP) return nclamp(a, 0, 1);
+    return nclamp(a - floorf(a), 0, 1);
+}
+DF C3 TexSample(const RtSceneView* S, int ti, V2 uv) {
+    const RtTexture t = S->textures[ti];
+    float u = Wrapper(uv.x, t.wrap), v = Wrapper(uv.y, t.wrap);
+    float fu = u * (float)(t.width - 1);
+    float fv = v * (float)(t.height - 1);
+    int pu = nf2i(fu), pv = nf2i(fv);
+    if (t.filter == RT_FILTER_LINEAR) {
+        int dpu = (fu > (float)pu + 0.5f) ? 1 : -1;
+        int dpv = (fv > (float)pv + 0.5f) ? 1 : -1;
+        int apu = nclampi(pu + dpu, 0, t.width - 1);
+        int apv = nclampi(pv + dpv, 0, t.height - 1);
+        float du = nmin(Abs(fu - (float)pu - 0.5f), 1);
+        float dv = nmin(Abs(fv - (float)pv - 0.5f), 1);
+        C3 a = TexRead(S, t, pu, pv), b = TexRead(S, t, apu, pv), c = TexRead(S, t, pu, apv), d = TexRead(S, t, apu, apv);
+        return (a * (1 - du) + b * du) * (1 - dv) + (c * (1 - du) + d * du) * dv;
+    }
+    return TexRead(S, t, pu, pv);
+}
+
+/* ---- shapes ----------------------------------------------------------------- */
+struct SurfPt { float u, v, t; };
+/* Moller-Trumbore exactly as Triangle.Intersect (Shapes/Triangle.cs:149-177) */
+DF bool TriTest(V3 pa, V3 e1, V3 e2, const Ray& ray, SurfPt* sp) {
+    V3 pvec = Cross(ray.D, e2);
+    float det = Dot(e1, pvec);
+    if (Abs(det) < kEps) return false;
+    float invDet = 1.0f / det;
+    V3 tvec = ray.O - pa;
+    float u = Dot(tvec, pvec) * invDet;
+    if (u < 0.0f || u > 1.0f) return false;
+    V3 qvec = Cross(tvec, e1);
+    float v = Dot(ray.D, qvec) * invDet;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    float t = Dot(e2, qvec) * invDet;
+    if (!(t >= ray.MinT && t <= ray.MaxT)) return false;
+    sp->u = u; sp->v = v; sp->t = t;
+    return true;
+}
+DF double dmin_(double a, double b) { if (a != b) { if (a == a) return a < b ? a : b; return a; } return signbit(a) ? a : b; }
+DF double dmax_(double a, double b) { if (a != b) { if (a == a) return b < a ? a : b; return a; } return signbit(b) ? a : b; }
+/* Sphere.Intersect (Shapes/Sphere.cs:65-80) with MathExt.SolveQuadratic in double */
+DF bool SphereTest(V3 c, float radius, const Ray& ray, float* tOut) {
+    double ox = (double)ray.O.x - (double)c.x, oy = (double)ray.O.y - (double)c.y, oz = (double)ray.O.z - (double)c.z;
+    double dx = ray.D.x, dy = ray.D.y, dz = ray.D.z;
+    double a = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    double b = __dmul_rn(2.0, __dadd_rn(__dadd_rn(__dmul_rn(ox, dx), __dmul_rn(oy, dy)), __dmul_rn(oz, dz)));
+    double cc = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(ox, ox), __dmul_rn(oy, oy)), __dmul_rn(oz, oz)), (double)Sqr(radius));
+    bool linearCase = a == 0.0;
+    bool validLinear = linearCase && b != 0.0;
+    double x0 = __ddiv_rn(-cc, b), x1 = x0;
+    double discrim = __dsub_rn(__dmul_rn(b, b), __dmul_rn(__dmul_rn(4.0, a), cc));
+    bool validQuadratic = !linearCase && (discrim >= 0.0);
+    if (validQuadratic) {
+        double root = __dsqrt_rn(discrim);
+        double temp = __dmul_rn(-0.5, __dadd_rn(b, copysign(root, b)));
+        double x0p = __ddiv_rn(temp, a), x1p = __ddiv_rn(cc, temp);
+        double x0m = dmin_(x0p, x1p), x1m = dmax_(x0p, x1p);
+        x0 = x0m; x1 = x1m;
+    }
+    bool found = validLinear || validQuadratic;
+    double mint = ray.MinT, maxt = ray.MaxT;
+    bool outB = !(x0 <= maxt && x1 >= mint);
+    bool inB = x0 < mint && x1 > maxt;
+    *tOut = x0 < mint ? (float)x1 : (float)x0;
+    return found && !outB && !inB;
+}
+
+/* triangle attributes at barycentrics (Triangle.GetIntersection / Sample) */
+DF void TriAttrs(const RtSceneView* S, int tri, V3 bary, V3* p, V3* n, V2* uv) {
+    RtTri t = S->tris[tri];
+    V3 pa = f4xyz(S->pos[t.v0]), pb = f4xyz(S->pos[t.v1]), pc = f4xyz(S->pos[t.v2]);
+    *p = bary.x * pa + bary.y * pb + bary.z * pc;
+    if (t.flags & 1) *n = Normalize(bary.x * f4xyz(S->nrm[t.v0]) + bary.y * f4xyz(S->nrm[t.v1]) + bary.z * f4xyz(S->nrm[t.v2]));
+    else *n = Normalize(Cross(pb - pa, pc - pa));
+    if (t.flags & 2) {
+        float2 a = S->uv[t.v0], b = S->uv[t.v1], c = S->uv[t.v2];
+        *uv = bary.x * v2(a.x, a.y) + bary.y * v2(b.x, b.y) + bary.z * v2(c.x, c.y);
+    } else {
+        *uv = bary.x * v2(0, 0) + bary.y * v2(1, 0) + bary.z * v2(1, 1);
+    }
+}
+DF V2 SphereUV(const RtSphere& s, V3 n) {
+    V3 local = XfN12(n, s.w2m);
+    float theta = rt_acosf(-local.y);
+    float phi = rt_atan2f(-local.z, local.x) + kPI;
+    return v2(phi / (2 * kPI), theta / kPI);
+}
+
+/* ---- Intersection (Intersection.cs) ------------------------------------------- */
+struct Isect {
+    V3 P; V2 UV; float T; Frame F; V3 Wr;
+    int prim;       /* top-level primitive id */
+    int sub;        /* instanced prototype primitive id or -1 */
+    int slot;       /* winning slot (absolute), for parity reporting */
+    float bu, bv;
+    uint32_t flags;
+};
+
+/* ---- BVH traversal ------------------------------------------------------------ */
+struct TravStats { uint32_t nodes, prims, insts; };
+
+struct Trav {
+    const RtSceneView* S;
+    uint32_t* status;
+    TravStats* st;
+    int2* stack;   /* 2 x RT_STACK_SIZE entries: top level, then instanced prototype */
+};
+
+/* Slab test (BoundingBox3F.cs:155-176) split into the part that does not
+ * depend on MaxT (returns false) and tMin; the caller compares tMin < MaxT.
+ * Gamma(3) is computed from float.Epsilon, a denormal, so 1 + 2*Gamma(3) == 1. */
+DF bool SlabA(float mnx, float mny, float mnz, float mxx, float mxy, float mxz, const Ray& r, float* tminOut) {
+    bool nx = r.InvD.x < 0, ny = r.InvD.y < 0, nz = r.InvD.z < 0;
+    float tMin = ((nx ? mxx : mnx) - r.O.x) * r.InvD.x;
+    float tMax = ((nx ? mnx : mxx) - r.O.x) * r.InvD.x;
+    float tyMin = ((ny ? mxy : mny) - r.O.y) * r.InvD.y;
+    float tyMax = ((ny ? mny : mxy) - r.O.y) * r.InvD.y;
+    if (tMin > tyMax || tyMin > tMax) return false;
+    if (tyMin > tMin) tMin = tyMin;
+    if (tyMax < tMax) tMax = tyMax;
+    float tzMin = ((nz ? mxz : mnz) - r.O.z) * r.InvD.z;
+    float tzMax = ((nz ? mnz : mxz) - r.O.z) * r.InvD.z;
+    if (tMin > tzMax || tzMin > tMax) return false;
+    if (tzMin > tMin) tMin = tzMin;
+    if (tzMax < tMax) tMax = tzMax;
+    *tminOut = tMin;
+    return tMax > 0;
+}
+
+/* closest-hit result inside one BVH */
+struct Best {
+    float t; float u, v; int slot; uint32_t flags;
+    int sub;         /* for instance candidates: winning prototype slot */
+    V3 pw;           /* for instance candidates: world-space point */
+};
+
+DF bool InstanceClosest(const RtSceneView* S, int inst, const Ray& ray, Best* b, int2* stack, uint32_t* status, TravStats* st);
+DF bool InstanceAny(const RtSceneView* S, int inst, const Ray& ray, int2* stack, uint32_t* status, TravStats* st);
+/* kTop: the top-level tree, whose leaves may be instances; a prototype tree
+ * (kTop = false) holds triangles and spheres only, which keeps the nesting
+ * one level deep at compile time. */
+
+/* One leaf primitive for the closest-hit traversal; updates ray.MaxT like
+ * Bvh.Intersect (Accelerators/Bvh.cs:193-204).  Returns true on a candidate hit. */
+template <bool kTop>
+DF void LeafClosest(const RtSceneView* S, int slot, Ray& ray, Best* best, bool* any, int2* stack, uint32_t* status, TravStats* st) {
+    float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
+    float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
+    float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
+    uint32_t kr = __float_as_uint(s1.w);
+    uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
+    if (st) st->prims++;
+    float t; float u = 0, v = 0; uint32_t fl = 0; int sub = -1; V3 pw = v3s(0);
+    if (kind == RT_KIND_TRI) {
+        SurfPt sp;
+        if (!TriTest(f4xyz(s0), f4xyz(s1), f4xyz(s2), ray, &sp)) return;
+        t = sp.t; u = sp.u; v = sp.v;
+    } else if (kind == RT_KIND_SPHERE) {
+        RtSphere sph = S->spheres[ref];
+        if (!SphereTest(v3(sph.center[0], sph.center[1], sph.center[2]), sph.radius, ray, &t)) return;
+    } else if (kTop) {
+        Best ib;
+        if (!InstanceClosest(S, (int)ref, ray, &ib, stack + RT_STACK_SIZE, status, st)) return;
+        t = ib.t; u = ib.u; v = ib.v; fl = ib.flags; sub = ib.slot; pw = ib.pw;
+    } else {
+        atomicOr(status, RT_STATUS_BADREF);
+        return;
+    }
+    *any = true;
+    best->flags |= fl;
+    if (t < best->t) {
+        best->t = t; best->u = u; best->v = v; best->slot = slot; best->sub = sub; best->pw = pw;
+        ray.MaxT = t;
+    } else if (t == best->t) {
+        best->flags |= RT_HIT_TIE;
+    }
+}
+
+/* Bvh.Intersect(ray, out inct) (Accelerators/Bvh.cs:174-232): the same set of
+ * boxes is tested in the same order against the same MaxT.  Both child boxes
+ * are read from the parent; the far child is pushed with its entry distance
+ * (or NaN when its slab test already failed) and re-checked against the MaxT
+ * current when it is popped, exactly when the reference would test it. */
+template <bool kTop>
+DF bool BvhClosest(const RtSceneView* S, int bvh, Ray& ray, Best* best, int2* stack, uint32_t* status, TravStats* st) {
+    const RtBvh h = S->bvhs[bvh];
+    best->t = kFMax; best->flags = 0; best->slot = -1; best->sub = -1; best->u = 0; best->v = 0;
+    if (h.root_ref == (int)0x80000000) return false;
+    bool any = false;
+    if (st) st->nodes++;
+    float tmin;
+    if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], ray, &tmin) || !(tmin < ray.MaxT))
+        return false;
+    const bool neg[3] = {ray.InvD.x < 0, ray.InvD.y < 0, ray.InvD.z < 0};
+    int sp = 0;
+    int cur = h.root_ref;
+    uint32_t guard = 0;
+    while (true) {
+        if (cur < 0) {
+            /* leaf */
+            int first = ~cur;
+            int count = __float_as_int(__ldg(S->slots + 3 * (int64_t)first + 2).w);
+            for (int i = 0; i < count; i++) LeafClosest<kTop>(S, first + i, ray, best, &any, stack, status, st);
+        } else {
+            if (++guard > (1u << 24)) { atomicOr(status, RT_STATUS_ITER); break; }
+            const float4* np = S->nodes + 4 * (int64_t)cur;
+            float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
+            float tl, tr;
+            bool al = SlabA(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ray, &tl);
+            bool ar = SlabA(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ray, &tr);
+            bool rightFirst = neg[axis];
+            int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
+            bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
+            float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
+            if (sp == RT_STACK_SIZE) { atomicOr(status, RT_STATUS_STACK); break; }
+            stack[sp++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
+            if (st) st->nodes++;
+            if (nearA && nearT < ray.MaxT) { cur = nearRef; continue; }
+        }
+        /* pop: the reference pops and tests the next box */
+        bool found = false;
+        while (sp > 0) {
+            int2 e = stack[--sp];
+            if (st) st->nodes++;
+            if (__int_as_float(e.y) < ray.MaxT) { cur = e.x; found = true; break; }
+        }
+        if (!found) break;
+    }
+    return any;
+}
+
+/* Bvh.Intersect(ray) any-hit (Accelerators/Bvh.cs:126-172) */
+template <bool kTop>
+DF bool BvhAny(const RtSceneView* S, int bvh, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
+    const RtBvh h = S->bvhs[bvh];
+    if (h.root_ref == (int)0x80000000) return false;
+    if (st) st->nodes++;
+    float tmin;
+    if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], ray, &tmin) || !(tmin < ray.MaxT))
+        return false;
+    const bool neg[3] = {ray.InvD.x < 0, ray.InvD.y < 0, ray.InvD.z < 0};
+    int sp = 0;
+    int cur = h.root_ref;
+    uint32_t guard = 0;
+    while (true) {
+        if (cur < 0) {
+            int first = ~cur;
+            int count = __float_as_int(__ldg(S->slots + 3 * (int64_t)first + 2).w);
+            for (int i = 0; i < count; i++) {
+                int slot = first + i;
+                float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
+                float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
+                float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
+                uint32_t kr = __float_as_uint(s1.w);
+                uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
+                if (st) st->prims++;
+                bool hit;
+                if (kind == RT_KIND_TRI) { SurfPt p; hit = TriTest(f4xyz(s0), f4xyz(s1), f4xyz(s2), ray, &p); }
+                else if (kind == RT_KIND_SPHERE) {
+                    RtSphere sph = S->spheres[ref]; float t;
+                    hit = SphereTest(v3(sph.center[0], sph.center[1], sph.center[2]), sph.radius, ray, &t);
+                } else if (kTop) {
+                    hit = InstanceAny(S, (int)ref, ray, stack + RT_STACK_SIZE, status, st);
+                } else {
+                    atomicOr(status, RT_STATUS_BADREF);
+                    hit = false;
+                }
+                if (hit) return true;
+            }
+        } else {
+            if (++guard > (1u << 24)) { atomicOr(status, RT_STATUS_ITER); return false; }
+            const float4* np = S->nodes + 4 * (int64_t)cur;
+            float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+            int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
+            float tl, tr;
+            bool al = SlabA(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ray, &tl);
+            bool ar = SlabA(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ray, &tr);
+            bool rightFirst = neg[axis];
+            int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
+            bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
+            float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
+            if (sp == RT_STACK_SIZE) { atomicOr(status, RT_STATUS_STACK); return false; }
+            stack[sp++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
+            if (st) st->nodes++;
+            if (nearA && nearT < ray.MaxT) { cur = nearRef; continue; }
+        }
+        bool found = false;
+        while (sp > 0) {
+            int2 e = stack[--sp];
+            if (st) st->nodes++;
+            if (__int_as_float(e.y) < ray.MaxT) { cur = e.x; found = true; break; }
+        }
+        if (!found) break;
+    }
+    return false;
+}
+
+/* InstancedPrimitive.Intersect (Primitive.cs:169-188): prototype traversal in
+ * model space, world T = Distance(ray.O, p). */
+DF bool InstanceClosest(const RtSceneView* S, int inst, const Ray& ray, Best* b, int2* stack, uint32_t* status, TravStats* st) {
+    if (st) st->insts++;
+    const RtInstance& I = S->instances[inst];
+    float w2m[12], m2w[12];
+#pragma unroll
+    for (int i = 0; i < 12; i++) { w2m[i] = __ldg(I.w2m + i); m2w[i] = __ldg(I.m2w + i); }
+    Ray mr = XfRay(ray, w2m);
+    Best mb;
+    if (!BvhClosest<false>(S, 1 + __ldg(&I.blas), mr, &mb, stack, status, st)) return false;
+    /* model-space point of the winning prototype primitive */
+    float4 s1 = __ldg(S->slots + 3 * (int64_t)mb.slot + 1);
+    uint32_t kr = __float_as_uint(s1.w);
+    V3 pm;
+    if ((kr >> RT_KIND_SHIFT) == RT_KIND_TRI) {
+        V3 bary = v3(1 - (mb.u + mb.v), mb.u, mb.v);
+        RtTri t = S->tris[kr & RT_REF_MASK];
+        pm = bary.x * f4xyz(S->pos[t.v0]) + bary.y * f4xyz(S->pos[t.v1]) + bary.z * f4xyz(S->pos[t.v2]);
+    } else {
+        RtSphere sph = S->spheres[kr & RT_REF_MASK];
+        V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
+        V3 n = Normalize(At(mr, mb.t) - c);
+        pm = n * sph.radius + c;
+    }
+    V3 pw = Xf12(pm, m2w);
+    b->t = Distance(ray.O, pw); b->u = mb.u; b->v = mb.v; b->slot = mb.slot; b->flags = mb.flags; b->pw = pw; b->sub = -1;
+    return true;
+}
+DF bool InstanceAny(const RtSceneView* S, int inst, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
+    if (st) st->insts++;
+    const RtInstance& I = S->instances[inst];
+    float w2m[12];
+#pragma unroll
+    for (int i = 0; i < 12; i++) w2m[i] = __ldg(I.w2m + i);
+    Ray mr = XfRay(ray, w2m);
+    return BvhAny<false>(S, 1 + __ldg(&I.blas), mr, stack, status, st);
+}
+
+/* Builds the full Intersection of the winning primitive (GetIntersection /
+ * InstancedPrimitive.Intersect). */
+DF void Finish(const RtSceneView* S, const Ray& ray, const Best& b, Isect* it) {
+    float4 s0 = __ldg(S->slots + 3 * (int64_t)b.slot);
+    float4 s1 = __ldg(S->slots + 3 * (int64_t)b.slot + 1);
+    uint32_t kr = __float_as_uint(s1.w);
+    uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
+    it->prim = __float_as_int(s0.w); it->sub = -1; it->slot = b.slot; it->flags = b.flags;
+    it->bu = b.u; it->bv = b.v;
+    if (kind == RT_KIND_TRI) {
+        V3 bary = v3(1 - (b.u + b.v), b.u, b.v);
+        V3 n;
+        TriAttrs(S, (int)ref, bary, &it->P, &n, &it->UV);
+        it->F = mkframe(n); it->T = b.t; it->Wr = -ray.D;
+    } else if (kind == RT_KIND_SPHERE) {
+        RtSphere sph = S->spheres[ref];
+        V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
+        V3 n = Normalize(At(ray, b.t) - c);
+        it->P = n * sph.radius + c; it->UV = SphereUV(sph, n); it->F = mkframe(n); it->T = b.t; it->Wr = -ray.D;
+    } else {
+        const RtInstance& I = S->instances[ref];
+        float w2m[12], m2w[12];
+        for (int i = 0; i < 12; i++) { w2m[i] = I.w2m[i]; m2w[i] = I.m2w[i]; }
+        V3 dm = Normalize(XfN12(ray.D, w2m));
+        float4 p0 = __ldg(S->slots + 3 * (int64_t)b.sub);
+        float4 p1 = __ldg(S->slots + 3 * (int64_t)b.sub + 1);
+        uint32_t pkr = __float_as_uint(p1.w);
+        V3 nm; V2 uvm;
+        if ((pkr >> RT_KIND_SHIFT) == RT_KIND_TRI) {
+            V3 bary = v3(1 - (b.u + b.v), b.u, b.v);
+            V3 pm;
+            TriAttrs(S, (int)(pkr & RT_REF_MASK), bary, &pm, &nm, &uvm);
+        } else {
+            /* sphere inside a prototype: normal from the model-space ray */
+            RtSphere sph = S->spheres[pkr & RT_REF_MASK];
+            Ray mr = XfRay(ray, w2m);
+            V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
+            float tm = 0; SphereTest(c, sph.radius, mr, &tm);
+            nm = Normalize(At(mr, tm) - c); uvm = SphereUV(sph, nm);
+        }
+        it->P = b.pw;
+        V3 n = Normalize(XfN12(nm, m2w));
+        it->F = mkframe(n);
+        it->Wr = Normalize(XfN12(-dm, m2w));
+        it->UV = uvm; it->T = b.t;
+        it->sub = __float_as_int(p0.w);
+    }
+}
+
+}  /* namespace rtd */
+
+#endif

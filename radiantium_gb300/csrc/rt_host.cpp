@@ -1,0 +1,758 @@
+/*
+ * rt_host.cpp - host runtime of the GB300 path tracer and the C ABI
+ * (include/radiantium.h).
+ *
+ * rt_upload_scene flattens the scene description exactly as
+ * RendererBuilder.Build orders it (RendererBuilder.cs:942-1004): primitives per
+ * entity (spheres, mesh triangles, instances), one DiffuseAreaLight per
+ * emissive primitive, infinite lights in entity order; builds the reference's
+ * SAH trees (rt_bvh.cpp) for every instanced prototype and the top level;
+ * and uploads the device layout of rt_types.h.  Compiled with
+ * -ffp-contract=off so derived values (edges, areas, centroids, CDFs) round
+ * exactly like the reference's single-precision code.
+ */
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits.h>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/radiantium.h"
+#include "../../include/rt_detmath.h"
+#include "rt_bvh.h"
+#include "rt_launch.h"
+#include "rt_types.h"
+
+namespace {
+
+struct RtFail : std::runtime_error {
+    int code;
+    RtFail(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess) throw RtFail(e_ == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, \
+                                            std::string(#x) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<DevBuf> scene_bufs;
+    RtSceneView view{};
+    RtSceneView* d_view = nullptr;             /* device copy of `view` handed to the kernels */
+    bool has_scene = false;
+    int width = 0, height = 0;
+    /* render scratch */
+    float* samples = nullptr; size_t samples_bytes = 0;
+    float* film = nullptr; size_t film_bytes = 0;
+    float* out = nullptr; size_t out_bytes = 0;
+    uint32_t* status = nullptr;
+    unsigned long long* stats = nullptr;
+    void* io = nullptr; size_t io_bytes = 0;   /* device staging for host-pointer calls */
+    bool counting = false;
+    rt_stats last{};
+    std::atomic<int> cancel{0};
+    int64_t sample_budget = 1 << 24;          /* samples per launch (sample buffer = 12 B each) */
+};
+
+void set_err(Ctx* c, const std::string& m) { if (c) c->err = m; }
+
+template <class T>
+T* upload(Ctx* c, const std::vector<T>& v) {
+    DevBuf b;
+    b.bytes = std::max<size_t>(sizeof(T), v.size() * sizeof(T));
+    CK(cudaMalloc(&b.p, b.bytes));
+    c->scene_bufs.push_back(b);
+    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return (T*)b.p;
+}
+
+void free_scene(Ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (DevBuf& b : c->scene_bufs) cudaFree(b.p);
+    c->scene_bufs.clear();
+    c->has_scene = false;
+    c->view = RtSceneView{};
+    c->d_view = nullptr;
+}
+
+template <class T>
+void ensure(T** p, size_t* have, size_t need) {
+    if (*have >= need && *p) return;
+    if (*p) cudaFree(*p);
+    *p = nullptr; *have = 0;
+    CK(cudaMalloc((void**)p, need));
+    *have = need;
+}
+
+/* ---- host float helpers with the kernels' operation order --------------- */
+struct F3 { float x, y, z; };
+inline F3 f3(float x, float y, float z) { F3 r{x, y, z}; return r; }
+inline F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline F3 cross(F3 a, F3 b) { return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline float length(F3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline F3 xform(F3 p, const float* m /* 16 */) {
+    return f3(p.x * m[0] + p.y * m[4] + p.z * m[8] + m[12],
+              p.x * m[1] + p.y * m[5] + p.z * m[9] + m[13],
+              p.x * m[2] + p.y * m[6] + p.z * m[10] + m[14]);
+}
+inline void rows12(const float* m16, float* m12) {
+    const int src[12] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
+    for (int i = 0; i < 12; i++) m12[i] = m16[src[i]];
+}
+inline F3 vertex(const rt_mesh_desc& m, int i) { return f3(m.positions[3 * i], m.positions[3 * i + 1], m.positions[3 * i + 2]); }
+
+/* TextureSampler.Sample on the host (environment luminance table) */
+inline int host_f2i(float f) {
+    if (f != f || f >= 2147483648.0f || f < -2147483648.0f) return INT_MIN;
+    return (int)f;
+}
+inline float hclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+inline int hclampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+inline float hmin(float a, float b) {
+    if (a != b) { if (a == a) return a < b ? a : b; return a; }
+    return std::signbit(a) ? a : b;
+}
+void tex_sample(const rt_texture_desc& t, float x, float y, float* rgb) {
+    auto wrap = [&](float a) { return t.wrap == RT_WRAP_CLAMP ? hclamp(a, 0, 1) : hclamp(a - std::floor(a), 0, 1); };
+    auto rd = [&](int px, int py, float* o) {
+        px = hclampi(px, 0, t.width - 1); py = hclampi(py, 0, t.height - 1);
+        const float* p = t.data + ((size_t)px * t.height + py) * 3;
+        o[0] = p[0]; o[1] = p[1]; o[2] = p[2];
+    };
+    float u = wrap(x), v = wrap(y);
+    float fu = u * (float)(t.width - 1), fv = v * (float)(t.height - 1);
+    int pu = host_f2i(fu), pv = host_f2i(fv);
+    if (t.filter == RT_FILTER_LINEAR) {
+        int dpu = (fu > (float)pu + 0.5f) ? 1 : -1, dpv = (fv > (float)pv + 0.5f) ? 1 : -1;
+        int apu = hclampi(pu + dpu, 0, t.width - 1), apv = hclampi(pv + dpv, 0, t.height - 1);
+        float du = hmin(std::fabs(fu - (float)pu - 0.5f), 1), dv = hmin(std::fabs(fv - (float)pv - 0.5f), 1);
+        float a[3], b[3], c[3], d[3];
+        rd(pu, pv, a); rd(apu, pv, b); rd(pu, apv, c); rd(apu, apv, d);
+        for (int k = 0; k < 3; k++) rgb[k] = (a[k] * (1 - du) + b[k] * du) * (1 - dv) + (c[k] * (1 - du) + d[k] * du) * dv;
+        return;
+    }
+    rd(pu, pv, rgb);
+}
+
+/* Distribution1D (Distribution1D.cs:19-49) appended to the pool */
+void dist1d(std::vector<float>& pool, const float* f, int n, int64_t* pdf_off, int64_t* cdf_off, float* integ) {
+    *pdf_off = (int64_t)pool.size();
+    pool.insert(pool.end(), f, f + n);
+    *cdf_off = (int64_t)pool.size();
+    std::vector<float> cdf(n + 1);
+    cdf[0] = 0;
+    for (int i = 1; i < n + 1; ++i) cdf[i] = cdf[i - 1] + f[i - 1] / (float)n;
+    float in = cdf[n];
+    if (in == 0) { for (int i = 1; i < n + 1; i++) cdf[i] = (float)i / (float)n; }
+    else { for (int i = 1; i < n + 1; i++) cdf[i] /= in; }
+    pool.insert(pool.end(), cdf.begin(), cdf.end());
+    *integ = in;
+}
+
+struct TopPrim {
+    int kind, ref, material, light, med_in, med_out;
+};
+
+void check_index(int i, int n, const char* what) {
+    if (i < 0 || i >= n) throw RtFail(RT_ERR_INVALID_ARG, std::string("scene: bad ") + what + " index " + std::to_string(i));
+}
+
+/* builds one BVH; appends nodes and slots; fills the header */
+void emit_bvh(const rtb::BuildResult& br, const std::vector<std::array<float4, 3>>& recs, std::vector<float4>& nodes,
+              std::vector<float4>& slots, RtBvh* hdr) {
+    const int slot_base = (int)(slots.size() / 3);
+    for (size_t i = 0; i < br.order.size(); i++) {
+        const std::array<float4, 3>& r = recs[br.order[i]];
+        slots.push_back(r[0]); slots.push_back(r[1]); slots.push_back(r[2]);
+    }
+    const std::vector<rtb::FlatNode>& fn = br.nodes;
+    if (fn.empty()) {
+        for (int k = 0; k < 3; k++) { hdr->root_min[k] = 0; hdr->root_max[k] = 0; }
+        hdr->root_ref = INT_MIN;
+        return;
+    }
+    /* interior nodes get consecutive device indices in depth-first order */
+    std::vector<int> dev(fn.size(), -1);
+    int node_base = (int)(nodes.size() / 4), nint = 0;
+    for (size_t i = 0; i < fn.size(); i++) if (fn[i].count == 0) dev[i] = node_base + nint++;
+    auto ref_of = [&](int i) -> int {
+        if (fn[i].count == 0) return dev[i];
+        int first = slot_base + fn[i].second;
+        if (fn[i].count > 65535) throw RtFail(RT_ERR_UNSUPPORTED, "BVH leaf with more than 65535 primitives");
+        float4& s2 = slots[3 * (size_t)first + 2];
+        int c = fn[i].count;
+        std::memcpy(&s2.w, &c, 4);
+        return ~first;
+    };
+    for (int k = 0; k < 3; k++) { hdr->root_min[k] = fn[0].bounds.mn[k]; hdr->root_max[k] = fn[0].bounds.mx[k]; }
+    hdr->root_ref = ref_of(0);
+    for (size_t i = 0; i < fn.size(); i++) {
+        if (fn[i].count != 0) { ref_of((int)i); continue; }
+        const rtb::Box& L = fn[i + 1].bounds;
+        const rtb::Box& R = fn[fn[i].second].bounds;
+        int lref = ref_of((int)i + 1), rref = ref_of(fn[i].second), axis = fn[i].axis;
+        float4 n0 = make_float4(L.mn[0], L.mn[1], L.mn[2], L.mx[0]);
+        float4 n1 = make_float4(L.mx[1], L.mx[2], R.mn[0], R.mn[1]);
+        float4 n2 = make_float4(R.mn[2], R.mx[0], R.mx[1], R.mx[2]);
+        float4 n3;
+        std::memcpy(&n3.x, &lref, 4); std::memcpy(&n3.y, &rref, 4); std::memcpy(&n3.z, &axis, 4); n3.w = 0;
+        nodes.push_back(n0); nodes.push_back(n1); nodes.push_back(n2); nodes.push_back(n3);
+    }
+}
+
+inline float4 f4bits(float x, float y, float z, int w) { float4 r = make_float4(x, y, z, 0); std::memcpy(&r.w, &w, 4); return r; }
+inline float4 f4bitsu(float x, float y, float z, uint32_t w) { float4 r = make_float4(x, y, z, 0); std::memcpy(&r.w, &w, 4); return r; }
+
+std::array<float4, 3> tri_rec(const rt_mesh_desc& m, int t, int prim_id, int global_tri) {
+    const int* ix = m.indices + 3 * (size_t)t;
+    F3 pa = vertex(m, ix[0]), pb = vertex(m, ix[1]), pc = vertex(m, ix[2]);
+    F3 e1 = sub(pb, pa), e2 = sub(pc, pa);
+    uint32_t kr = ((uint32_t)RT_KIND_TRI << RT_KIND_SHIFT) | (uint32_t)global_tri;
+    return {f4bits(pa.x, pa.y, pa.z, prim_id), f4bitsu(e1.x, e1.y, e1.z, kr), f4bits(e2.x, e2.y, e2.z, 0)};
+}
+std::array<float4, 3> other_rec(int kind, int ref, int prim_id) {
+    uint32_t kr = ((uint32_t)kind << RT_KIND_SHIFT) | (uint32_t)ref;
+    return {f4bits(0, 0, 0, prim_id), f4bitsu(0, 0, 0, kr), f4bits(0, 0, 0, 0)};
+}
+rtb::Box tri_box(const rt_mesh_desc& m, int t) {
+    const int* ix = m.indices + 3 * (size_t)t;
+    F3 pa = vertex(m, ix[0]), pb = vertex(m, ix[1]), pc = vertex(m, ix[2]);
+    rtb::Box b;
+    b.mn[0] = b.mx[0] = pa.x; b.mn[1] = b.mx[1] = pa.y; b.mn[2] = b.mx[2] = pa.z;
+    float q[3] = {pb.x, pb.y, pb.z}; rtb::box_expand(b, q);
+    float r[3] = {pc.x, pc.y, pc.z}; rtb::box_expand(b, r);
+    return b;
+}
+rtb::Box sphere_box(const rt_sphere_desc& s) {
+    rtb::Box b;
+    for (int k = 0; k < 3; k++) { b.mn[k] = s.center[k] - s.radius; b.mx[k] = s.center[k] + s.radius; }
+    return b;
+}
+/* BoundingBox3F.Transform (BoundingBox3F.cs:232-244) */
+rtb::Box xform_box(const rtb::Box& b, const float* m) {
+    const float* mn = b.mn; const float* mx = b.mx;
+    F3 c[8] = {f3(mn[0], mn[1], mn[2]), f3(mx[0], mn[1], mn[2]), f3(mn[0], mx[1], mn[2]), f3(mn[0], mn[1], mx[2]),
+               f3(mn[0], mx[1], mx[2]), f3(mx[0], mx[1], mn[2]), f3(mx[0], mn[1], mx[2]), f3(mx[0], mx[1], mx[2])};
+    F3 p = xform(c[0], m);
+    rtb::Box r;
+    r.mn[0] = r.mx[0] = p.x; r.mn[1] = r.mx[1] = p.y; r.mn[2] = r.mx[2] = p.z;
+    for (int i = 1; i < 8; i++) { F3 q = xform(c[i], m); float v[3] = {q.x, q.y, q.z}; rtb::box_expand(r, v); }
+    return r;
+}
+
+void upload_scene(Ctx* c, const rt_scene_desc* d) {
+    if (!d || d->abi_version != RT_ABI_VERSION) throw RtFail(RT_ERR_INVALID_ARG, "scene: null descriptor or ABI version mismatch");
+    if (d->camera.width <= 0 || d->camera.height <= 0) throw RtFail(RT_ERR_INVALID_ARG, "scene: camera resolution must be positive");
+    const int threads = std::max(1u, std::thread::hardware_concurrency());
+    const int maxp = d->bvh_max_prims < 1 ? 1 : d->bvh_max_prims;
+
+    /* global vertex / triangle tables: every mesh, in mesh order */
+    std::vector<float4> pos, nrm;
+    std::vector<float2> uvs;
+    std::vector<RtTri> tris;
+    std::vector<int> mesh_tri_base(d->mesh_count), mesh_vtx_base(d->mesh_count);
+    for (int m = 0; m < d->mesh_count; m++) {
+        const rt_mesh_desc& md = d->meshes[m];
+        if (md.vertex_count < 0 || md.triangle_count < 0 || (md.triangle_count > 0 && (!md.positions || !md.indices)))
+            throw RtFail(RT_ERR_INVALID_ARG, "scene: mesh " + std::to_string(m) + " has no positions / indices");
+        mesh_vtx_base[m] = (int)pos.size();
+        mesh_tri_base[m] = (int)tris.size();
+        for (int i = 0; i < md.vertex_count; i++) {
+            pos.push_back(make_float4(md.positions[3 * i], md.positions[3 * i + 1], md.positions[3 * i + 2], 0));
+            nrm.push_back(md.normals ? make_float4(md.normals[3 * i], md.normals[3 * i + 1], md.normals[3 * i + 2], 0) : make_float4(0, 0, 0, 0));
+            uvs.push_back(md.uvs ? make_float2(md.uvs[2 * i], md.uvs[2 * i + 1]) : make_float2(0, 0));
+        }
+        for (int t = 0; t < md.triangle_count; t++) {
+            RtTri tr;
+            for (int k = 0; k < 3; k++) {
+                int vi = md.indices[3 * t + k];
+                if (vi < 0 || vi >= md.vertex_count) throw RtFail(RT_ERR_INVALID_ARG, "scene: mesh " + std::to_string(m) + " index out of range");
+            }
+            tr.v0 = mesh_vtx_base[m] + md.indices[3 * t];
+            tr.v1 = mesh_vtx_base[m] + md.indices[3 * t + 1];
+            tr.v2 = mesh_vtx_base[m] + md.indices[3 * t + 2];
+            tr.flags = (md.normals ? 1 : 0) | (md.uvs ? 2 : 0);
+            tris.push_back(tr);
+        }
+    }
+    std::vector<RtSphere> spheres(d->sphere_count);
+    for (int i = 0; i < d->sphere_count; i++) {
+        const rt_sphere_desc& s = d->spheres[i];
+        for (int k = 0; k < 3; k++) spheres[i].center[k] = s.center[k];
+        spheres[i].radius = s.radius;
+        rows12(s.world_to_model, spheres[i].w2m);
+    }
+    for (int i = 0; i < d->material_count; i++) {
+        const rt_material_desc& m = d->materials[i];
+        bool needR = m.type != RT_MAT_ROUGH_METAL, needT = m.type == RT_MAT_ROUGH_GLASS || m.type == RT_MAT_PERFECT_GLASS;
+        bool needRough = m.type == RT_MAT_ROUGH_METAL || m.type == RT_MAT_ROUGH_GLASS || m.type == RT_MAT_ROUGH_PLASTIC;
+        auto ok = [&](int t) { return t >= 0 && t < d->texture_count; };
+        if (m.type < 0 || m.type > RT_MAT_PERFECT_GLASS || (needR && !ok(m.tex_r)) || (needT && !ok(m.tex_t)) ||
+            (needRough && (!ok(m.tex_roughness) || !ok(m.tex_anisotropic))))
+            throw RtFail(RT_ERR_INVALID_ARG, "scene: material " + std::to_string(i) + " is missing a texture or has an unknown type");
+    }
+
+    std::vector<float4> nodes, slots;
+    std::vector<RtBvh> bvhs(1 + d->blas_count);
+    /* instanced prototypes: ShapeWrapperPrimitive per shape (RendererBuilder.cs:895-921) */
+    std::vector<rtb::Box> blas_root(d->blas_count);
+    for (int b = 0; b < d->blas_count; b++) {
+        int first = d->blas_ranges[2 * b], count = d->blas_ranges[2 * b + 1];
+        if (first < 0 || count < 0 || first + count > d->blas_group_count) throw RtFail(RT_ERR_INVALID_ARG, "scene: bad prototype range");
+        std::vector<rtb::Box> boxes;
+        std::vector<std::array<float4, 3>> recs;
+        for (int g = first; g < first + count; g++) {
+            const rt_group_desc& gd = d->blas_groups[g];
+            if (gd.kind == RT_GROUP_SPHERE) {
+                check_index(gd.ref, d->sphere_count, "sphere");
+                boxes.push_back(sphere_box(d->spheres[gd.ref]));
+                recs.push_back(other_rec(RT_KIND_SPHERE, gd.ref, (int)recs.size()));
+            } else if (gd.kind == RT_GROUP_MESH) {
+                check_index(gd.ref, d->mesh_count, "mesh");
+                const rt_mesh_desc& md = d->meshes[gd.ref];
+                for (int t = 0; t < md.triangle_count; t++) {
+                    boxes.push_back(tri_box(md, t));
+                    recs.push_back(tri_rec(md, t, (int)recs.size(), mesh_tri_base[gd.ref] + t));
+                }
+            } else {
+                throw RtFail(RT_ERR_INVALID_ARG, "scene: instanced prototype groups must be meshes or spheres");
+            }
+        }
+        rtb::BuildResult br = rtb::build_sah(boxes, maxp, threads);
+        emit_bvh(br, recs, nodes, slots, &bvhs[1 + b]);
+        if (!br.nodes.empty()) blas_root[b] = br.nodes[0].bounds;
+        else blas_root[b] = rtb::empty_box();
+    }
+
+    /* top level, lights, infinite lights */
+    std::vector<rtb::Box> boxes;
+    std::vector<std::array<float4, 3>> recs;
+    std::vector<RtPrim> prims;
+    std::vector<RtLight> lights;
+    std::vector<int32_t> infinite;
+    std::vector<RtInstance> insts;
+    auto area_light = [&](int kind, int ref, const rt_group_desc& gd, float area) {
+        RtLight L{};
+        L.kind = kind; L.ref = ref; L.le[0] = gd.le[0]; L.le[1] = gd.le[1]; L.le[2] = gd.le[2]; L.area = area;
+        L.dist = -1;
+        lights.push_back(L);
+        return (int)lights.size() - 1;
+    };
+    for (int g = 0; g < d->group_count; g++) {
+        const rt_group_desc& gd = d->groups[g];
+        if (gd.material >= d->material_count || gd.medium_inside >= d->medium_count || gd.medium_outside >= d->medium_count)
+            throw RtFail(RT_ERR_INVALID_ARG, "scene: group " + std::to_string(g) + " references a missing material / medium");
+        TopPrim tp{0, 0, gd.material < 0 ? -1 : gd.material, -1, gd.medium_inside < 0 ? -1 : gd.medium_inside,
+                   gd.medium_outside < 0 ? -1 : gd.medium_outside};
+        switch (gd.kind) {
+        case RT_GROUP_INFINITE_LIGHT: {
+            check_index(gd.ref, d->texture_count, "texture");
+            RtLight L{};
+            L.kind = RT_LIGHT_INFINITE; L.ref = gd.ref;
+            rows12(gd.model_to_world, L.m2w); rows12(gd.world_to_model, L.w2m);
+            L.dist = -1;
+            infinite.push_back((int)lights.size());
+            lights.push_back(L);
+            break;
+        }
+        case RT_GROUP_SPHERE: {
+            check_index(gd.ref, d->sphere_count, "sphere");
+            const rt_sphere_desc& s = d->spheres[gd.ref];
+            int id = (int)prims.size();
+            int li = -1;
+            if (gd.emissive) li = area_light(RT_LIGHT_AREA_SPHERE, gd.ref, gd, 4 * s.radius * s.radius * 3.14159265f);
+            prims.push_back(RtPrim{RT_KIND_SPHERE, gd.ref, tp.material, li, tp.med_in, tp.med_out, 0, 0});
+            boxes.push_back(sphere_box(s));
+            recs.push_back(other_rec(RT_KIND_SPHERE, gd.ref, id));
+            break;
+        }
+        case RT_GROUP_MESH: {
+            check_index(gd.ref, d->mesh_count, "mesh");
+            const rt_mesh_desc& md = d->meshes[gd.ref];
+            for (int t = 0; t < md.triangle_count; t++) {
+                int id = (int)prims.size();
+                int gt = mesh_tri_base[gd.ref] + t;
+                int li = -1;
+                if (gd.emissive) {
+                    const int* ix = md.indices + 3 * (size_t)t;
+                    F3 pa = vertex(md, ix[0]), pb = vertex(md, ix[1]), pc = vertex(md, ix[2]);
+                    float area = 0.5f * length(cross(sub(pb, pa), sub(pc, pa)));
+                    li = area_light(RT_LIGHT_AREA_TRI, gt, gd, area);
+                }
+                prims.push_back(RtPrim{RT_KIND_TRI, gt, tp.material, li, tp.med_in, tp.med_out, 0, 0});
+                boxes.push_back(tri_box(md, t));
+                recs.push_back(tri_rec(md, t, id, gt));
+            }
+            break;
+        }
+        case RT_GROUP_INSTANCE: {
+            check_index(gd.ref, d->blas_count, "instanced prototype");
+            RtInstance I{};
+            rows12(gd.model_to_world, I.m2w); rows12(gd.world_to_model, I.w2m);
+            I.blas = gd.ref;
+            int id = (int)prims.size();
+            prims.push_back(RtPrim{RT_KIND_INSTANCE, (int)insts.size(), tp.material, -1, tp.med_in, tp.med_out, 0, 0});
+            boxes.push_back(xform_box(blas_root[gd.ref], gd.model_to_world));
+            recs.push_back(other_rec(RT_KIND_INSTANCE, (int)insts.size(), id));
+            insts.push_back(I);
+            break;
+        }
+        default:
+            throw RtFail(RT_ERR_INVALID_ARG, "scene: unknown group kind " + std::to_string(gd.kind));
+        }
+    }
+    if (prims.empty()) throw RtFail(RT_ERR_INVALID_ARG, "scene: no primitives");
+    rtb::BuildResult top = rtb::build_sah(boxes, maxp, threads);
+    emit_bvh(top, recs, nodes, slots, &bvhs[0]);
+
+    /* textures */
+    std::vector<RtTexture> texs(d->texture_count);
+    std::vector<float> texels;
+    for (int i = 0; i < d->texture_count; i++) {
+        const rt_texture_desc& t = d->textures[i];
+        if (t.width <= 0 || t.height <= 0 || !t.data) throw RtFail(RT_ERR_INVALID_ARG, "scene: bad texture " + std::to_string(i));
+        texs[i].width = t.width; texs[i].height = t.height; texs[i].wrap = t.wrap; texs[i].filter = t.filter;
+        texs[i].offset = (int64_t)texels.size();
+        texels.insert(texels.end(), t.data, t.data + (size_t)t.width * t.height * 3);
+    }
+    /* infinite lights: luminance * sin(theta) table and Distribution2D (InfiniteAreaLight.cs:21-54),
+     * world sphere from the top-level bounds (Light.cs:181-187) */
+    std::vector<RtDist2D> dists;
+    std::vector<float> pool;
+    const rtb::Box& wb = top.nodes[0].bounds;
+    for (int li : infinite) {
+        RtLight& L = lights[li];
+        const rt_texture_desc& t = d->textures[L.ref];
+        const int W = t.width, H = t.height;
+        std::vector<float> lum((size_t)W * H);
+        for (int y = 0; y < H; y++) {
+            float sinTheta = rt_sinf(((float)y + 0.5f) / (float)H * 3.14159265f);
+            float v = (float)y / (float)H;
+            for (int x = 0; x < W; x++) {
+                float u = (float)x / (float)W;
+                float rgb[3];
+                tex_sample(t, u, v, rgb);
+                lum[(size_t)y * W + x] = (rgb[0] * 0.212671f + rgb[1] * 0.715160f + rgb[2] * 0.072169f) * sinTheta;
+            }
+        }
+        RtDist2D D{};
+        D.nu = W; D.nv = H;
+        std::vector<float> cond_int(H);
+        std::vector<float> cond_pdf_cdf;
+        D.cond_pdf = (int64_t)pool.size();
+        pool.insert(pool.end(), lum.begin(), lum.end());
+        D.cond_cdf = (int64_t)pool.size();
+        for (int y = 0; y < H; y++) {
+            const float* f = lum.data() + (size_t)y * W;
+            std::vector<float> cdf(W + 1);
+            cdf[0] = 0;
+            for (int i = 1; i < W + 1; ++i) cdf[i] = cdf[i - 1] + f[i - 1] / (float)W;
+            float in = cdf[W];
+            if (in == 0) { for (int i = 1; i < W + 1; i++) cdf[i] = (float)i / (float)W; }
+            else { for (int i = 1; i < W + 1; i++) cdf[i] /= in; }
+            pool.insert(pool.end(), cdf.begin(), cdf.end());
+            cond_int[y] = in;
+        }
+        D.cond_int = (int64_t)pool.size();
+        pool.insert(pool.end(), cond_int.begin(), cond_int.end());
+        dist1d(pool, cond_int.data(), H, &D.marg_pdf, &D.marg_cdf, &D.marg_int);
+        L.dist = (int)dists.size();
+        dists.push_back(D);
+        float cx = (wb.mx[0] + wb.mn[0]) * 0.5f, cy = (wb.mx[1] + wb.mn[1]) * 0.5f, cz = (wb.mx[2] + wb.mn[2]) * 0.5f;
+        L.world_center[0] = cx; L.world_center[1] = cy; L.world_center[2] = cz;
+        F3 dg = f3(wb.mx[0] - wb.mn[0], wb.mx[1] - wb.mn[1], wb.mx[2] - wb.mn[2]);
+        L.world_radius = length(dg) / 2.0f;
+    }
+    std::vector<RtMaterial> mats(d->material_count);
+    for (int i = 0; i < d->material_count; i++) {
+        const rt_material_desc& m = d->materials[i];
+        RtMaterial& o = mats[i];
+        o.type = m.type; o.dist = m.dist; o.two_sided = m.two_sided;
+        o.tex_r = m.tex_r; o.tex_t = m.tex_t; o.tex_rough = m.tex_roughness; o.tex_anis = m.tex_anisotropic;
+        o.eta_a = m.eta_a; o.eta_b = m.eta_b; o.kd = m.kd; o.ks = m.ks;
+        for (int k = 0; k < 3; k++) { o.eta[k] = m.eta[k]; o.k[k] = m.k[k]; }
+    }
+    std::vector<RtMedium> meds(d->medium_count);
+    for (int i = 0; i < d->medium_count; i++) {
+        const rt_medium_desc& m = d->media[i];
+        for (int k = 0; k < 3; k++) {
+            meds[i].sig_a[k] = m.sigma_a[k] * m.scale;
+            meds[i].sig_s[k] = m.sigma_s[k] * m.scale;
+            meds[i].sig_t[k] = meds[i].sig_a[k] + meds[i].sig_s[k];
+        }
+        meds[i].g = m.g;
+    }
+    if (d->global_medium >= d->medium_count) throw RtFail(RT_ERR_INVALID_ARG, "scene: bad global medium");
+
+    free_scene(c);
+    RtSceneView& v = c->view;
+    v.nodes = upload(c, nodes);
+    v.slots = upload(c, slots);
+    v.bvhs = upload(c, bvhs);
+    v.prims = upload(c, prims);
+    v.tris = upload(c, tris);
+    v.pos = upload(c, pos);
+    v.nrm = upload(c, nrm);
+    v.uv = upload(c, uvs);
+    v.spheres = upload(c, spheres);
+    v.instances = upload(c, insts);
+    v.materials = upload(c, mats);
+    v.textures = upload(c, texs);
+    v.texels = upload(c, texels);
+    v.media = upload(c, meds);
+    v.lights = upload(c, lights);
+    v.infinite_lights = upload(c, infinite);
+    v.dists = upload(c, dists);
+    v.dist_pool = upload(c, pool);
+    v.light_count = (int)lights.size();
+    v.infinite_count = (int)infinite.size();
+    v.global_medium = d->global_medium < 0 ? -1 : d->global_medium;
+    RtCamera& cam = v.camera;
+    cam.width = d->camera.width; cam.height = d->camera.height;
+    cam.near_z = d->camera.near_z; cam.far_z = d->camera.far_z;
+    cam.inv_res_x = 1.0f / (float)cam.width; cam.inv_res_y = 1.0f / (float)cam.height;
+    std::memcpy(cam.clip_to_camera, d->camera.clip_to_camera, sizeof(cam.clip_to_camera));
+    std::memcpy(cam.camera_to_world, d->camera.camera_to_world, sizeof(cam.camera_to_world));
+    c->d_view = upload(c, std::vector<RtSceneView>{v});
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_scene = true;
+    c->width = cam.width; c->height = cam.height;
+}
+
+void check_status(Ctx* c) {
+    uint32_t st = 0;
+    CK(cudaMemcpyAsync(&st, c->status, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
+    if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
+    if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
+}
+
+void read_stats(Ctx* c) {
+    unsigned long long s[8];
+    CK(cudaMemcpyAsync(s, c->stats, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->last.rays_closest = s[1]; c->last.rays_shadow = s[2]; c->last.node_visits = s[3];
+    c->last.prim_tests = s[4]; c->last.instance_visits = s[5]; c->last.invalid_samples = s[6];
+}
+
+void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaStream_t user) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (!p || !dst || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render: null params/output or spp <= 0");
+    if (p->integrator != RT_INTEGRATOR_PATH && p->integrator != RT_INTEGRATOR_VOL_PATH) throw RtFail(RT_ERR_INVALID_ARG, "render: unknown integrator");
+    RtParams P{};
+    P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
+    P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;
+    P.seed = p->seed; P.x0 = p->x0; P.y0 = p->y0;
+    P.w = p->width > 0 ? p->width : c->width - p->x0;
+    P.h = p->height > 0 ? p->height : c->height - p->y0;
+    if (P.x0 < 0 || P.y0 < 0 || P.w <= 0 || P.h <= 0 || P.x0 + P.w > c->width || P.y0 + P.h > c->height)
+        throw RtFail(RT_ERR_INVALID_ARG, "render: crop outside the film");
+    P.spp = p->spp; P.sample_begin = p->sample_begin;
+    cudaStream_t s = user ? user : c->stream;
+    const int64_t npix = (int64_t)P.w * P.h;
+    int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(P.spp, c->sample_budget / std::max<int64_t>(1, npix)));
+    ensure(&c->samples, &c->samples_bytes, (size_t)npix * chunk * 12);
+    ensure(&c->film, &c->film_bytes, (size_t)npix * 12);
+    CK(cudaMemsetAsync(c->film, 0, (size_t)npix * 12, s));
+    CK(cudaMemsetAsync(c->status, 0, 4, s));
+    CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
+    c->cancel.store(0);
+    for (int b = 0; b < P.spp; b += chunk) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        P.chunk_begin = b;
+        P.chunk_len = std::min(chunk, P.spp - b);
+        CK(rt_launch_render(c->d_view, P, c->samples, c->status, c->stats, c->counting, s));
+        CK(rt_launch_accumulate(c->film, c->samples, npix, P.chunk_len, s));
+    }
+    float* out = dst;
+    if (dst_host) {
+        ensure(&c->out, &c->out_bytes, (size_t)npix * 12);
+        out = c->out;
+    }
+    CK(rt_launch_finalize(out, c->film, npix, (float)P.spp, s));
+    if (dst_host) CK(cudaMemcpyAsync(dst, out, (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    check_status(c);
+    std::memset(&c->last, 0, sizeof(c->last));
+    read_stats(c);
+    c->last.samples = (uint64_t)npix * P.spp;
+}
+
+void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (n < 0 || (n > 0 && (!rays || (!hits && !occ)))) throw RtFail(RT_ERR_INVALID_ARG, "trace: bad arguments");
+    cudaStream_t s = user ? user : c->stream;
+    CK(cudaMemsetAsync(c->status, 0, 4, s));
+    CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
+    const rt_ray* dr = rays;
+    rt_hit* dh = hits;
+    uint8_t* dob = occ;
+    if (host && n > 0) {
+        size_t out_bytes = hits ? (size_t)n * sizeof(rt_hit) : (size_t)n;
+        ensure(&c->io, &c->io_bytes, (size_t)n * sizeof(rt_ray) + out_bytes + 256);
+        char* base = (char*)c->io;
+        CK(cudaMemcpyAsync(base, rays, (size_t)n * sizeof(rt_ray), cudaMemcpyHostToDevice, s));
+        dr = (const rt_ray*)base;
+        char* ob = base + (((size_t)n * sizeof(rt_ray) + 255) & ~(size_t)255);
+        if (hits) dh = (rt_hit*)ob; else dob = (uint8_t*)ob;
+    }
+    CK(rt_launch_trace(c->d_view, dr, n, dh, dob, c->status, c->stats, c->counting, s));
+    if (host && n > 0) {
+        if (hits) CK(cudaMemcpyAsync(hits, dh, (size_t)n * sizeof(rt_hit), cudaMemcpyDeviceToHost, s));
+        else CK(cudaMemcpyAsync(occ, dob, (size_t)n, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    check_status(c);
+    std::memset(&c->last, 0, sizeof(c->last));
+    read_stats(c);
+    if (hits) c->last.rays_closest = (uint64_t)n; else c->last.rays_shadow = (uint64_t)n;
+}
+
+template <class F>
+int run(Ctx* c, F f) {
+    if (!c) return RT_ERR_INVALID_ARG;
+    try {
+        CK(cudaSetDevice(c->device));
+        f();
+        c->err.clear();
+        return RT_OK;
+    } catch (const RtFail& e) {
+        c->err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        c->err = "host allocation failed";
+        return RT_ERR_OOM;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return RT_ERR_INVALID_ARG;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rt_abi_version(void) { return RT_ABI_VERSION; }
+
+int rt_create(int device, void** out_ctx) {
+    if (!out_ctx) return RT_ERR_INVALID_ARG;
+    *out_ctx = nullptr;
+    Ctx* c = new (std::nothrow) Ctx();
+    if (!c) return RT_ERR_OOM;
+    c->device = device;
+    int rc = run(c, [&]() {
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        CK(cudaMalloc((void**)&c->status, 4));
+        CK(cudaMalloc((void**)&c->stats, 8 * sizeof(unsigned long long)));
+    });
+    if (rc != RT_OK) { delete c; return rc; }
+    *out_ctx = c;
+    return RT_OK;
+}
+
+void rt_destroy(void* ctx) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return;
+    cudaSetDevice(c->device);
+    free_scene(c);
+    if (c->samples) cudaFree(c->samples);
+    if (c->film) cudaFree(c->film);
+    if (c->out) cudaFree(c->out);
+    if (c->io) cudaFree(c->io);
+    if (c->status) cudaFree(c->status);
+    if (c->stats) cudaFree(c->stats);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* rt_last_error(const void* ctx) {
+    const Ctx* c = (const Ctx*)ctx;
+    return c ? c->err.c_str() : "null context";
+}
+
+int rt_upload_scene(void* ctx, const rt_scene_desc* scene) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { upload_scene(c, scene); });
+}
+
+int rt_trace_closest(void* ctx, const rt_ray* rays, int64_t n, rt_hit* hits) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { if (!hits && n > 0) throw RtFail(RT_ERR_INVALID_ARG, "null hits"); trace(c, rays, n, hits, nullptr, true, nullptr); });
+}
+int rt_trace_any(void* ctx, const rt_ray* rays, int64_t n, uint8_t* occluded) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { if (!occluded && n > 0) throw RtFail(RT_ERR_INVALID_ARG, "null output"); trace(c, rays, n, nullptr, occluded, true, nullptr); });
+}
+int rt_trace_closest_device(void* ctx, const rt_ray* d_rays, int64_t n, rt_hit* d_hits, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { if (!d_hits && n > 0) throw RtFail(RT_ERR_INVALID_ARG, "null hits"); trace(c, d_rays, n, d_hits, nullptr, false, (cudaStream_t)stream); });
+}
+int rt_trace_any_device(void* ctx, const rt_ray* d_rays, int64_t n, uint8_t* d_occ, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { if (!d_occ && n > 0) throw RtFail(RT_ERR_INVALID_ARG, "null output"); trace(c, d_rays, n, nullptr, d_occ, false, (cudaStream_t)stream); });
+}
+int rt_render(void* ctx, const rt_render_params* params, float* out_rgb) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render(c, params, out_rgb, true, nullptr); });
+}
+int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render(c, params, d_out_rgb, false, (cudaStream_t)stream); });
+}
+int rt_get_stats(void* ctx, rt_stats* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !out) return RT_ERR_INVALID_ARG;
+    *out = c->last;
+    return RT_OK;
+}
+int rt_set_counting(void* ctx, int enabled) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return RT_ERR_INVALID_ARG;
+    c->counting = enabled != 0;
+    return RT_OK;
+}
+int rt_cancel(void* ctx) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return RT_ERR_INVALID_ARG;
+    c->cancel.store(1);
+    return RT_OK;
+}
+
+/* test hook (not part of radiantium.h): runs rt_detmath (fn 0..7) or CUDA's
+ * own functions (fn 100..107) on the device over host arrays */
+int rt_debug_detmath(void* ctx, int fn, const float* a, const float* b, float* out, int64_t n) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() {
+        float* d = nullptr;
+        CK(cudaMalloc((void**)&d, (size_t)n * 12 + 16));
+        cudaError_t e = cudaSuccess;
+        e = cudaMemcpyAsync(d, a, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + n, b, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = rt_launch_detmath(fn, d, d + n, d + 2 * n, n, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + 2 * n, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(d);
+        CK(e);
+    });
+}
+
+}  /* extern "C" */

@@ -1,0 +1,20 @@
+/*
+ * rt_launch.h - host-callable launchers of the kernels in rt_kernels.cu.
+ */
+#ifndef RT_LAUNCH_H
+#define RT_LAUNCH_H
+#include <cuda_runtime.h>
+#include "rt_types.h"
+#include "../../include/radiantium.h"
+
+/* stats slots: 0 samples, 1 closest rays, 2 shadow rays, 3 node visits,
+ * 4 primitive tests, 5 instance visits, 6 invalid samples */
+cudaError_t rt_launch_render(const RtSceneView* S, const RtParams& P, float* samples, uint32_t* status,
+                             unsigned long long* stats, bool counting, cudaStream_t stream);
+cudaError_t rt_launch_accumulate(float* film, const float* samples, int64_t npix, int chunk_len, cudaStream_t stream);
+cudaError_t rt_launch_finalize(float* out, const float* film, int64_t npix, float spp, cudaStream_t stream);
+cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ,
+                            uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
+cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream);
+
+#endif

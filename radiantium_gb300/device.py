@@ -1,0 +1,113 @@
+"""Python binding of the CUDA library through its C ABI (include/radiantium.h).
+
+:class:`Device` owns one rt context (one CUDA stream) and one uploaded scene.
+Every call goes through ``libradiantium_gb300.so``; a missing library raises
+(there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native as N
+from .scene import RenderSettings, SceneDesc
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Device:
+    """An rt context on one GPU: upload a scene, trace ray batches, render."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.load_library()
+        h = C.c_void_p()
+        rc = self.lib.rt_create(device, C.byref(h))
+        if rc != N.RT_OK:
+            raise N.RTError(rc, "rt_create failed (is a CUDA device visible?)")
+        self.h = h
+        self.scene: SceneDesc | None = None
+        self._packed = None
+
+    def _check(self, rc: int):
+        if rc != N.RT_OK:
+            raise N.RTError(rc, self.lib.rt_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, scene: SceneDesc):
+        packed = scene.to_c()
+        self._check(self.lib.rt_upload_scene(self.h, C.byref(packed.desc)))
+        self.scene, self._packed = scene, packed
+
+    def set_counting(self, on: bool):
+        self._check(self.lib.rt_set_counting(self.h, 1 if on else 0))
+
+    def stats(self) -> dict:
+        st = N.Stats()
+        self._check(self.lib.rt_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def cancel(self):
+        self._check(self.lib.rt_cancel(self.h))
+
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=N.ray_dtype())
+        hits = np.zeros(rays.shape[0], dtype=N.hit_dtype())
+        self._check(self.lib.rt_trace_closest(self.h, _ptr(rays), rays.shape[0], _ptr(hits)))
+        return hits
+
+    def trace_any(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=N.ray_dtype())
+        occ = np.zeros(rays.shape[0], dtype=np.uint8)
+        self._check(self.lib.rt_trace_any(self.h, _ptr(rays), rays.shape[0], _ptr(occ)))
+        return occ
+
+    def _crop(self, s: RenderSettings):
+        cam = self.scene.camera
+        return (s.width or cam.width - s.x0), (s.height or cam.height - s.y0)
+
+    def render(self, settings: RenderSettings) -> np.ndarray:
+        """Averaged film of the crop, ColorBuffer layout (x, y, rgb)."""
+        w, h = self._crop(settings)
+        out = np.zeros(w * h * 3, dtype=np.float32)
+        p = settings.to_c()
+        self._check(self.lib.rt_render(self.h, C.byref(p), _ptr(out)))
+        return out.reshape(w, h, 3)
+
+    def render_device(self, settings: RenderSettings, out_ptr: int, stream: int = 0):
+        """Film written to device memory `out_ptr` (w*h*3 float32) on `stream` (0 = context stream)."""
+        p = settings.to_c()
+        self._check(self.lib.rt_render_device(self.h, C.byref(p), C.c_void_p(out_ptr), C.c_void_p(stream or None)))
+
+    def trace_closest_device(self, rays_ptr: int, n: int, hits_ptr: int, stream: int = 0):
+        self._check(self.lib.rt_trace_closest_device(self.h, C.c_void_p(rays_ptr), n, C.c_void_p(hits_ptr),
+                                                     C.c_void_p(stream or None)))
+
+    def detmath(self, fn: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:
+        """Runs the deterministic math (fn 0..7) or CUDA's own functions (fn 100..107) on the GPU."""
+        f = self.lib.rt_debug_detmath
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        b = np.ascontiguousarray(a if b is None else b, dtype=np.float32)
+        out = np.empty_like(a)
+        self._check(f(self.h, fn, _ptr(a), _ptr(b), _ptr(out), a.size))
+        return out

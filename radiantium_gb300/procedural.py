@@ -236,3 +236,69 @@ WORKLOADS = {
     "instanced": instanced_spheres,
     "volume": volume_sphere,
 }
+
+
+def material_zoo(width=64, height=64, seed=3):
+    """Small test scene exercising every material plugin, both area-light shapes,
+    instancing and an environment light (parity tests, not a benchmark)."""
+    s = SceneDesc(camera=Camera.look_at(width, height, 50.0, (0.0, 1.4, 4.2), (0.0, 0.6, 0.0)), name="zoo")
+    zero = s.add_const(0.0)
+    one = s.add_const(1.0)
+    white = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.7, 0.7, 0.7))))
+    checker = np.zeros((8, 8, 3), dtype=np.float32)
+    checker[(np.add.outer(np.arange(8), np.arange(8)) % 2) == 0] = (0.8, 0.3, 0.2)
+    checker[(np.add.outer(np.arange(8), np.arange(8)) % 2) == 1] = (0.2, 0.3, 0.8)
+    ck = s.add_texture(Texture.from_image_hw3(checker, N.WRAP_REPEAT, N.FILTER_LINEAR))
+    two = s.add_material(Material(N.MAT_DIFFUSE, tex_r=ck, two_sided=True))
+    metal = s.add_material(Material(N.MAT_ROUGH_METAL, N.DIST_GGX, tex_roughness=s.add_const(0.4),
+                                    tex_anisotropic=s.add_const(0.3), eta=CU_ETA, k=CU_K))
+    metal_b = s.add_material(Material(N.MAT_ROUGH_METAL, N.DIST_BECKMANN, tex_roughness=s.add_const(0.3),
+                                      tex_anisotropic=zero, eta=CU_ETA, k=CU_K))
+    glass = s.add_material(Material(N.MAT_ROUGH_GLASS, N.DIST_GGX, tex_r=one, tex_t=one, tex_roughness=s.add_const(0.25),
+                                    tex_anisotropic=zero, eta_a=1.0, eta_b=1.5))
+    plastic = s.add_material(Material(N.MAT_ROUGH_PLASTIC, N.DIST_GGX, tex_r=s.add_const((0.2, 0.6, 0.3)),
+                                      tex_roughness=s.add_const(0.3), tex_anisotropic=zero, kd=0.6, ks=0.4))
+    plastic_b = s.add_material(Material(N.MAT_ROUGH_PLASTIC, N.DIST_BECKMANN, tex_r=s.add_const((0.6, 0.5, 0.2)),
+                                        tex_roughness=s.add_const(0.2), tex_anisotropic=s.add_const(-0.4)))
+    mirror = s.add_material(Material(N.MAT_PERFECT_MIRROR, tex_r=s.add_const((0.9, 0.9, 0.9))))
+    pglass = s.add_material(Material(N.MAT_PERFECT_GLASS, tex_r=one, tex_t=one))
+    lightmat = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const(0.5)))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(quad((-3, 0, -3), (-3, 0, 3), (3, 0, 3), (3, 0, -3))), material=two))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(quad((-3, 0, -2), (3, 0, -2), (3, 3, -2), (-3, 3, -2))), material=white))
+    from .scene import Sphere
+    for i, (m, x) in enumerate([(metal, -1.6), (glass, -0.55), (plastic, 0.55), (pglass, 1.6)]):
+        s.spheres.append(Sphere((x, 0.45, 0.0), 0.45))
+        s.groups.append(Group(N.GROUP_SPHERE, len(s.spheres) - 1, material=m))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(box_mesh((-1.0, 0.3, 1.1), (0.5, 0.6, 0.5), 25.0)), material=mirror))
+    proto = s.add_mesh(displaced_sphere(6, seed, amplitude=0.1))
+    s.blas.append([Group(N.GROUP_MESH, proto)])
+    for j, (m, x) in enumerate([(metal_b, 0.4), (plastic_b, 1.3)]):
+        m2w = Mat4.scale((0.35, 0.35, 0.35)) * Mat4.from_axis_angle((0, 1, 0), 0.7 * j) * Mat4.translation((x, 0.35, 1.2))
+        s.groups.append(Group(N.GROUP_INSTANCE, 0, material=m, model_to_world=m2w))
+    light = quad((-0.5, 2.8, -0.5), (0.5, 2.8, -0.5), (0.5, 2.8, 0.5), (-0.5, 2.8, 0.5))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(light), material=lightmat, emissive=True, le=(8.0, 8.0, 8.0)))
+    s.spheres.append(Sphere((2.2, 2.2, 0.5), 0.15))
+    s.groups.append(Group(N.GROUP_SPHERE, len(s.spheres) - 1, material=lightmat, emissive=True, le=(30.0, 20.0, 10.0)))
+    env = s.add_texture(gaussian_lobe_env(64, 32, seed, lobes=4))
+    s.groups.append(Group(N.GROUP_INFINITE_LIGHT, env, model_to_world=Mat4.from_axis_angle((0, 1, 0), 0.3)))
+    settings = RenderSettings(N.INTEGRATOR_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=6, min_depth=2,
+                              rr_threshold=0.99, spp=4, seed=5)
+    return s, settings
+
+
+def volume_box(width=64, height=64, seed=9):
+    """Small vol_path test scene: a global medium, a medium-filled displaced sphere
+    with no material, a glass sphere, diffuse ground and one area light."""
+    s, st = volume_sphere(width, height, sphere_n=6, seed=seed)
+    s.global_medium = s.add_medium(Medium((0.01, 0.02, 0.03), (0.05, 0.05, 0.05), g=-0.3, scale=1.0))
+    one = s.add_const(1.0)
+    zero = s.add_const(0.0)
+    glass = s.add_material(Material(N.MAT_ROUGH_GLASS, N.DIST_GGX, tex_r=one, tex_t=one, tex_roughness=s.add_const(0.2),
+                                    tex_anisotropic=zero, eta_a=1.0, eta_b=1.5))
+    from .scene import Sphere
+    s.spheres.append(Sphere((1.6, 0.5, 0.3), 0.5))
+    s.groups.append(Group(N.GROUP_SPHERE, len(s.spheres) - 1, material=glass, medium_outside=s.global_medium))
+    for g in s.groups:
+        if g.kind == N.GROUP_MESH and g.material >= 0:
+            g.medium_outside = s.global_medium
+    return s, st.replace(spp=4, max_depth=12)
