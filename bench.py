@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 path tracer on the reference's headline workload.
+
+Workload (default `instanced`): plain `path` integrator with MIS over 64
+instances of a ~200k-triangle displaced sphere (GGX conductors with
+alpha ~ U[0.05, 0.5] and rough dielectrics of IOR 1.5) lit by a 1024x512 HDR
+environment of 8 Gaussian lobes; 1024x1024 pixels, 256 samples per pixel,
+max depth 8.  The scene is generated from a seed (the reference ships none).
+
+A step renders one progressive pass of `--spp-per-step` samples per pixel over
+the whole film (the reference's BlockBasedRenderer sample loop, continued with
+`sample_begin`), so the default 16 steps x 16 spp render exactly the 256-spp
+frame.  `value` is device-resident throughput (samples/s) timed with CUDA
+events; `e2e` renders the same passes through the C ABI call a host binding
+makes (rt_render, film copied back to pinned host memory every step).
+
+`--impl reference` times the reference's CPU path restated in C++ (oracle/,
+all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "samples/s at fixed relMSE, batched vs plain GPU path; adjoint grads/s vs FD"
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                "clocks_event_reasons.sw_power_cap")
+# algorithmic bytes (reference layout): ray record in + hit out per traced ray,
+# one 32-byte LinearBVHNode per box test, 48 bytes per primitive test
+# (3 indices + 3 positions), two 4x4 matrices per instance traversal,
+# one 12-byte film write per sample.
+B_RAY, B_NODE, B_PRIM, B_INST, B_FILM = 48, 32, 48, 128, 12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["instanced", "cornell", "volume"], default="instanced")
+    ap.add_argument("--spp-per-step", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront"], default="auto")
+    ap.add_argument("--plain-steps", type=int, default=2,
+                    help="steps of the plain megakernel timed in the same run for the batched/plain ratio (0: skip)")
+    return ap.parse_args()
+
+
+def workload(name):
+    from radiantium_gb300 import procedural
+    scene, st = {"instanced": procedural.instanced_spheres, "cornell": procedural.cornell_box,
+                 "volume": procedural.volume_sphere}[name]()
+    return scene, st
+
+
+def workload_config(name, scene, st, spp_step):
+    from radiantium_gb300 import native as N
+    return {
+        "workload": {"instanced": "path MIS, 64 instances of a displaced sphere (GGX conductor / rough dielectric), "
+                                  "1024x512 Gaussian-lobe env",
+                     "cornell": "path MIS, procedural Cornell box (36 tris, ceiling quad light)",
+                     "volume": "vol_path, displaced sphere bounding a homogeneous medium, ground, quad light"}[name],
+        "film": [scene.camera.width, scene.camera.height],
+        "spp_frame": st.spp,
+        "spp_per_step": spp_step,
+        "max_depth": st.max_depth,
+        "integrator": "vol_path" if st.integrator == N.INTEGRATOR_VOL_PATH else "path",
+        "triangles": scene.triangle_count,
+        "seed": st.seed,
+    }
+
+
+def cpu_baseline(scene, st, target_s, threads=0):
+    """Times the CPU oracle (the reference path restated in C++) on a bounded
+    centre crop of the same workload, all host cores."""
+    from oracle.oracle import OracleScene
+    cores = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    orc = OracleScene(scene)
+    build_s = time.perf_counter() - t0
+    w = min(64, scene.camera.width)
+    h = min(64, scene.camera.height)
+    x0, y0 = (scene.camera.width - w) // 2, (scene.camera.height - h) // 2
+    cal = st.replace(spp=1, x0=x0, y0=y0, width=w, height=h)
+    t0 = time.perf_counter()
+    orc.render(cal, threads=cores)
+    t1 = time.perf_counter() - t0
+    spp = int(max(1, min(st.spp, target_s / max(t1, 1e-3))))
+    run = cal.replace(spp=spp)
+    t0 = time.perf_counter()
+    orc.render(run, threads=cores)
+    dt = time.perf_counter() - t0
+    samples = w * h * spp
+    orc.close()
+    return {"value": samples / dt, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": f"centre {w}x{h} crop x {spp} spp of the same workload ({samples} samples, {dt:.1f} s; "
+                      f"oracle scene build {build_s:.1f} s not timed)"}
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={CLOCK_FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, reasons, mx = [], set(), None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def profiled_traffic(name):
+    """Per-sample DRAM traffic of the path-tracing kernel from the committed ncu
+    summary (profiles/k_render_<workload>_traffic.txt: one line `bytes_per_sample=<x>`)."""
+    p = os.path.join(ROOT, "profiles", f"k_render_{name}_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("bytes_per_sample="):
+            return float(line.split("=", 1)[1])
+    return None
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    scene, st = workload(args.workload)
+    from oracle.oracle import OracleScene
+    cores = os.cpu_count() or 1
+    orc = OracleScene(scene)
+    w = min(64, scene.camera.width)
+    h = min(64, scene.camera.height)
+    x0, y0 = (scene.camera.width - w) // 2, (scene.camera.height - h) // 2
+    cal = st.replace(spp=1, x0=x0, y0=y0, width=w, height=h)
+    t0 = time.perf_counter()
+    orc.render(cal, threads=cores)
+    t1 = time.perf_counter() - t0
+    # each step: a bounded sample sized so the whole run stays within a few minutes
+    total_steps = args.steps + args.warmup
+    spp = int(max(1, min(st.spp, (150.0 / total_steps) / max(t1, 1e-3))))
+    step = cal.replace(spp=spp)
+    for i in range(args.warmup):
+        orc.render(step.replace(sample_begin=i * spp), threads=cores)
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        orc.render(step.replace(sample_begin=(args.warmup + i) * spp), threads=cores)
+        times.append(time.perf_counter() - t0)
+    samples = w * h * spp
+    ms = 1000.0 * float(np.mean(times))
+    value = samples / (ms / 1000.0)
+    sample_desc = f"centre {w}x{h} crop x {spp} spp per step ({samples} samples/step)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": dict(workload_config(args.workload, scene, st, spp), step=sample_desc),
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
+                         "sample": sample_desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
+                                                 "(oracle/) runs on all host cores"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from radiantium_gb300.device import Device
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from radiantium_gb300 import native as N
+    scene, st = workload(args.workload)
+    t0 = time.perf_counter()
+    dev = Device(local)
+    dev.upload(scene)
+    mode = {"auto": N.RENDERER_AUTO, "megakernel": N.RENDERER_MEGAKERNEL, "wavefront": N.RENDERER_WAVEFRONT}[args.renderer]
+    dev.set_renderer(mode)
+    uses_wavefront = mode == N.RENDERER_WAVEFRONT or (
+        mode == N.RENDERER_AUTO and st.integrator == N.INTEGRATOR_PATH and st.strategy == N.STRATEGY_UNIFORM)
+    upload_s = time.perf_counter() - t0
+    W, H = scene.camera.width, scene.camera.height
+    npix = W * H
+    spp_step = args.spp_per_step
+    # each rank renders its own sample passes (independent, no exchange): weak scaling
+    base = rank * (args.warmup + args.steps) * spp_step
+    film = torch.empty(npix * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    # one untimed counting pass: exact traversal counts of this workload
+    dev.set_counting(True)
+    dev.render_device(st.replace(spp=spp_step, sample_begin=base), film.data_ptr(), stream)
+    torch.cuda.synchronize()
+    counts = dev.stats()
+    dev.set_counting(False)
+
+    for i in range(args.warmup):
+        dev.render_device(st.replace(spp=spp_step, sample_begin=base + i * spp_step), film.data_ptr(), stream)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, kernel_ms, shade_ms, launches, render_launches = [], 0.0, 0.0, 0, 0
+    for i in range(args.steps):
+        flush.fill_(float(i))  # L2 flush between timed steps, outside the events
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dev.render_device(st.replace(spp=spp_step, sample_begin=base + (args.warmup + i) * spp_step),
+                          film.data_ptr(), stream)
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        s = dev.stats()
+        kernel_ms += s["render_kernel_ms"]
+        shade_ms += s["shade_kernel_ms"]
+        launches += s["kernel_launches"]
+        render_launches += s["render_launches"]
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    samples_step = npix * spp_step
+    value = samples_step * world / (ms_step / 1000.0)
+
+    # e2e: the C ABI call a host binding makes, film copied to pinned host memory each step
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(npix * 3, dtype=torch.float32, pin_memory=True).numpy()
+        import ctypes as C
+        p = host.ctypes.data_as(C.c_void_p)
+        lib, h = dev.lib, dev.h
+        times = []
+        for i in range(args.steps):
+            prm = st.replace(spp=spp_step, sample_begin=base + (args.warmup + args.steps + i) * spp_step).to_c()
+            t0 = time.perf_counter()
+            rc = lib.rt_render(h, C.byref(prm), p)
+            times.append(time.perf_counter() - t0)
+            if rc != 0:
+                raise RuntimeError(lib.rt_last_error(h).decode())
+        e2e_s = float(np.mean(times))
+        e2e = {"value": samples_step * world / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": npix * 12,
+               "note": "rt_render with a pinned host film; scene resident (rt_upload_scene once, "
+                       f"{upload_s:.2f} s incl. BVH builds)"}
+
+    # the plain megakernel on the same passes, for the wavefront / megakernel ratio
+    plain = None
+    if uses_wavefront and args.plain_steps > 0:
+        dev.set_renderer(N.RENDERER_MEGAKERNEL)
+        pt = []
+        for i in range(args.plain_steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.render_device(st.replace(spp=spp_step, sample_begin=base + (args.warmup + i) * spp_step),
+                              film.data_ptr(), stream)
+            e1.record()
+            e1.synchronize()
+            pt.append(e0.elapsed_time(e1))
+        dev.set_renderer(mode)
+        plain = {"value": samples_step / (float(np.mean(pt)) / 1000.0), "unit": "samples/s", "steps": args.plain_steps,
+                 "note": "plain megakernel (one thread per camera sample), same passes, identical films"}
+
+    # roofline of the path-tracing kernel (algorithmic bytes from exact counts)
+    alg_bytes_step = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
+                      + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"] + B_FILM * counts["samples"])
+    # wavefront: every traversal launch of a step together traces the step's rays,
+    # so the roofline uses the step's algorithmic bytes over its summed traversal time
+    launches_per_step = max(1, render_launches // args.steps)
+    launch_ms = kernel_ms / max(1, render_launches)
+    achieved = alg_bytes_step / (kernel_ms / args.steps / 1000.0) / 1e9
+    peak, peak_src = measured_peak()
+    tps = profiled_traffic(args.workload)
+    traffic = None if tps is None else tps * samples_step / launches_per_step
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, st, args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": dict(workload_config(args.workload, scene, st, spp_step),
+                       parallelism=f"replicas x{world} (independent sample passes)",
+                       l2="256 MiB flush between timed steps (outside the CUDA events)",
+                       renderer=("wavefront (trace / shade kernels over compacted queues, path regeneration)"
+                                 if uses_wavefront else "plain megakernel (one thread per camera sample)")),
+        "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src,
+                     "kernel": "k_wf_trace" if uses_wavefront else "k_render",
+                     "alg_bytes_per_launch": alg_bytes_step / launches_per_step, "launch_ms": launch_ms,
+                     "launches_per_step": launches_per_step,
+                     "kernel_ms_per_step": kernel_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
+        "plain_megakernel": plain,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
+                                                   "prim_tests", "instance_visits", "invalid_samples")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dev.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -224,7 +224,12 @@ typedef struct rt_stats {
     uint64_t prim_tests;      /* primitive intersection tests */
     uint64_t instance_visits; /* instanced-prototype traversals */
     uint64_t invalid_samples; /* Color3F.IsValid == false, zeroed (BlockBasedRenderer.cs:141-145) */
-    uint64_t reserved[5];
+    uint64_t kernel_launches; /* kernels this library launched for the call */
+    uint64_t render_launches; /* of which path-tracing launches */
+    double render_kernel_ms;  /* summed duration of the path-tracing launches (CUDA events on their stream):
+                                 the megakernel, or the wavefront traversal kernel */
+    double shade_kernel_ms;   /* wavefront shading kernel (0 for the megakernel) */
+    uint64_t reserved[1];
 } rt_stats;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -275,6 +280,15 @@ int rt_get_stats(void* ctx, rt_stats* out);
 /* Enables per-ray counters (node visits, primitive tests) in later calls:
  * the counting build of the kernels, used for the roofline's algorithmic bytes. */
 int rt_set_counting(void* ctx, int enabled);
+
+/* Selects the render pipeline: RT_RENDERER_AUTO (wavefront where it applies,
+ * i.e. the `path` integrator with the Uniform light strategy; megakernel
+ * otherwise), RT_RENDERER_MEGAKERNEL or RT_RENDERER_WAVEFRONT.  Both produce
+ * identical films; this is the GpuWavefrontRenderer "renderer" option. */
+#define RT_RENDERER_AUTO 0
+#define RT_RENDERER_MEGAKERNEL 1
+#define RT_RENDERER_WAVEFRONT 2
+int rt_set_renderer(void* ctx, int mode);
 
 /* Requests cancellation of a running render (Renderer.Stop, BlockBasedRenderer.cs:85-88). */
 int rt_cancel(void* ctx);

@@ -38,6 +38,8 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
     objs = {
         "rt_kernels.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_kernels.cu")],
+        "rt_wavefront.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                            "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_wavefront.cu")],
         "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                       f"-I{cuda}/include", "-c", os.path.join(CSRC, "rt_host.cpp")],
         "rt_bvh.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",

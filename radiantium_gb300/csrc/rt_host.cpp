@@ -30,6 +30,7 @@
 #include "rt_bvh.h"
 #include "rt_launch.h"
 #include "rt_types.h"
+#include "rt_wavefront.h"
 
 namespace {
 
@@ -70,7 +71,24 @@ struct Ctx {
     rt_stats last{};
     std::atomic<int> cancel{0};
     int64_t sample_budget = 1 << 24;          /* samples per launch (sample buffer = 12 B each) */
+    std::vector<cudaEvent_t> events;           /* per-launch timing of the path-tracing kernel */
+    int renderer = RT_RENDERER_AUTO;
+    /* wavefront path state */
+    WfState wf{};
+    std::vector<DevBuf> wf_bufs;
+    int wf_slots = 0;
+    int32_t* wf_counters = nullptr;            /* [0] rays queued, [1] / [2] active lists */
+    int32_t* h_counts = nullptr;               /* pinned mirror of wf_counters */
+    int wf_capacity = 1 << 21;                 /* path slots in flight */
 };
+
+void ensure_events(Ctx* c, size_t n) {
+    while (c->events.size() < n) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c->events.push_back(e);
+    }
+}
 
 void set_err(Ctx* c, const std::string& m) { if (c) c->err = m; }
 
@@ -100,6 +118,46 @@ void ensure(T** p, size_t* have, size_t need) {
     *p = nullptr; *have = 0;
     CK(cudaMalloc((void**)p, need));
     *have = need;
+}
+
+template <class T>
+T* wf_alloc(Ctx* c, size_t n) {
+    DevBuf b;
+    b.bytes = std::max<size_t>(sizeof(T), n * sizeof(T));
+    CK(cudaMalloc(&b.p, b.bytes));
+    c->wf_bufs.push_back(b);
+    return (T*)b.p;
+}
+
+void free_wf(Ctx* c) {
+    for (DevBuf& b : c->wf_bufs) cudaFree(b.p);
+    c->wf_bufs.clear();
+    c->wf = WfState{};
+    c->wf_slots = 0;
+}
+
+/* path-state arrays for `slots` paths in flight (about 300 bytes per slot) */
+void ensure_wf(Ctx* c, int slots) {
+    if (c->wf_slots >= slots) return;
+    free_wf(c);
+    WfState& W = c->wf;
+    const size_t n = (size_t)slots, q = 3 * (size_t)slots;
+    W.q_o = wf_alloc<float4>(c, q); W.q_d = wf_alloc<float4>(c, q); W.q_meta = wf_alloc<int32_t>(c, q);
+    W.active = wf_alloc<int32_t>(c, n); W.active_next = wf_alloc<int32_t>(c, n);
+    W.next_sample = wf_alloc<unsigned long long>(c, 1);
+    W.pix = wf_alloc<int4>(c, n); W.rng_n = wf_alloc<uint32_t>(c, n);
+    W.coeff = wf_alloc<float4>(c, n); W.rad = wf_alloc<float4>(c, n);
+    W.bounce = wf_alloc<int2>(c, n); W.flags = wf_alloc<uint32_t>(c, n);
+    W.ray_o = wf_alloc<float4>(c, n); W.ray_d = wf_alloc<float4>(c, n);
+    W.pd_coeff = wf_alloc<float4>(c, n); W.pd_l1 = wf_alloc<float4>(c, n); W.pd_fr = wf_alloc<float4>(c, n);
+    W.pd_mis = wf_alloc<float4>(c, n); W.pd_w = wf_alloc<float4>(c, n);
+    W.pd_ray_o = wf_alloc<float4>(c, n); W.pd_ray_d = wf_alloc<float4>(c, n);
+    W.ext_hit = wf_alloc<float4>(c, n); W.ext_sub = wf_alloc<int32_t>(c, n);
+    W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
+    W.occluded = wf_alloc<uint8_t>(c, n);
+    if (!c->wf_counters) CK(cudaMalloc((void**)&c->wf_counters, 4 * sizeof(int32_t)));
+    if (!c->h_counts) CK(cudaMallocHost((void**)&c->h_counts, 4 * sizeof(int32_t)));
+    c->wf_slots = slots;
 }
 
 /* ---- host float helpers with the kernels' operation order --------------- */
@@ -554,6 +612,9 @@ void read_stats(Ctx* c) {
     c->last.prim_tests = s[4]; c->last.instance_visits = s[5]; c->last.invalid_samples = s[6];
 }
 
+void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s);
+void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s);
+
 void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaStream_t user) {
     if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
     if (!p || !dst || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render: null params/output or spp <= 0");
@@ -576,12 +637,13 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
-    for (int b = 0; b < P.spp; b += chunk) {
-        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-        P.chunk_begin = b;
-        P.chunk_len = std::min(chunk, P.spp - b);
-        CK(rt_launch_render(c->d_view, P, c->samples, c->status, c->stats, c->counting, s));
-        CK(rt_launch_accumulate(c->film, c->samples, npix, P.chunk_len, s));
+    const bool uniform_path = P.integrator == RT_INTEGRATOR_PATH && P.strategy == RT_STRATEGY_UNIFORM;
+    if (c->renderer == RT_RENDERER_WAVEFRONT && !uniform_path)
+        throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs the path integrator with the Uniform light strategy");
+    if (c->renderer == RT_RENDERER_WAVEFRONT || (c->renderer == RT_RENDERER_AUTO && uniform_path)) {
+        render_wavefront(c, P, chunk, npix, s);
+    } else {
+        render_megakernel(c, P, chunk, npix, s);
     }
     float* out = dst;
     if (dst_host) {
@@ -592,9 +654,100 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     if (dst_host) CK(cudaMemcpyAsync(dst, out, (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     check_status(c);
+    double rms = c->last.render_kernel_ms, sms = c->last.shade_kernel_ms;
+    uint64_t launches = c->last.kernel_launches, rl = c->last.render_launches;
     std::memset(&c->last, 0, sizeof(c->last));
     read_stats(c);
     c->last.samples = (uint64_t)npix * P.spp;
+    c->last.render_kernel_ms = rms;
+    c->last.shade_kernel_ms = sms;
+    c->last.render_launches = rl;
+    c->last.kernel_launches = launches + 1;
+}
+
+void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
+    const int nchunks = (P.spp + chunk - 1) / chunk;
+    ensure_events(c, 2 * (size_t)nchunks);
+    uint64_t launches = 0;
+    for (int b = 0, ci = 0; b < P.spp; b += chunk, ci++) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        P.chunk_begin = b;
+        P.chunk_len = std::min(chunk, P.spp - b);
+        CK(cudaEventRecord(c->events[2 * ci], s));
+        CK(rt_launch_render(c->d_view, P, c->samples, c->status, c->stats, c->counting, s));
+        CK(cudaEventRecord(c->events[2 * ci + 1], s));
+        CK(rt_launch_accumulate(c->film, c->samples, npix, P.chunk_len, s));
+        launches += 2;
+    }
+    CK(cudaStreamSynchronize(s));
+    double ms = 0;
+    for (int ci = 0; ci < nchunks; ci++) {
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, c->events[2 * ci], c->events[2 * ci + 1]));
+        ms += t;
+    }
+    c->last.render_kernel_ms = ms;
+    c->last.shade_kernel_ms = 0;
+    c->last.render_launches = (uint64_t)nchunks;
+    c->last.kernel_launches = launches;
+}
+
+/* wavefront: trace all queued rays, shade all active paths, repeat until
+ * every sample of the chunk has finished (rt_wavefront.cu) */
+void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
+    const int64_t max_samples = npix * (int64_t)chunk;
+    const int slots = (int)std::min<int64_t>(c->wf_capacity, max_samples + 31);
+    ensure_wf(c, slots);
+    ensure_events(c, 4);
+    WfState W = c->wf;
+    W.samples = c->samples;
+    W.n_rays_next = c->wf_counters;
+    double trace_ms = 0, shade_ms = 0;
+    uint64_t launches = 0, trace_launches = 0;
+    for (int b = 0; b < P.spp; b += chunk) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        P.chunk_begin = b;
+        P.chunk_len = std::min(chunk, P.spp - b);
+        W.n_active = c->wf_counters + 1;
+        W.n_active_next = c->wf_counters + 2;
+        W.active = c->wf.active;
+        W.active_next = c->wf.active_next;
+        CK(cudaMemsetAsync(c->wf_counters, 0, 4 * sizeof(int32_t), s));
+        CK(cudaMemsetAsync(W.next_sample, 0, sizeof(unsigned long long), s));
+        CK(rt_wf_start(c->d_view, P, W, slots, s));
+        launches += 2;
+        CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        int n_rays = c->h_counts[0], n_active = c->h_counts[1];
+        while (n_active > 0) {
+            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+            CK(cudaEventRecord(c->events[0], s));
+            CK(rt_wf_trace(c->d_view, W, n_rays, c->status, c->stats, c->counting, s));
+            CK(cudaEventRecord(c->events[1], s));
+            CK(cudaMemsetAsync(W.n_rays_next, 0, sizeof(int32_t), s));
+            CK(cudaMemsetAsync(W.n_active_next, 0, sizeof(int32_t), s));
+            CK(cudaEventRecord(c->events[2], s));
+            CK(rt_wf_shade(c->d_view, P, W, n_active, c->status, c->stats, c->counting, true, s));
+            CK(cudaEventRecord(c->events[3], s));
+            launches += (n_rays > 0 ? 1 : 0) + 1;
+            trace_launches += n_rays > 0 ? 1 : 0;
+            std::swap(W.active, W.active_next);
+            std::swap(W.n_active, W.n_active_next);
+            CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            n_rays = c->h_counts[0];
+            n_active = c->h_counts[W.n_active - c->wf_counters];
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
+            CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+        }
+        CK(rt_launch_accumulate(c->film, c->samples, npix, P.chunk_len, s));
+        launches += 1;
+    }
+    c->last.render_kernel_ms = trace_ms;
+    c->last.shade_kernel_ms = shade_ms;
+    c->last.render_launches = trace_launches;
+    c->last.kernel_launches = launches;
 }
 
 void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
@@ -625,6 +778,7 @@ void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bo
     std::memset(&c->last, 0, sizeof(c->last));
     read_stats(c);
     if (hits) c->last.rays_closest = (uint64_t)n; else c->last.rays_shadow = (uint64_t)n;
+    c->last.kernel_launches = n > 0 ? 1 : 0;
 }
 
 template <class F>
@@ -680,6 +834,10 @@ void rt_destroy(void* ctx) {
     if (c->io) cudaFree(c->io);
     if (c->status) cudaFree(c->status);
     if (c->stats) cudaFree(c->stats);
+    free_wf(c);
+    if (c->wf_counters) cudaFree(c->wf_counters);
+    if (c->h_counts) cudaFreeHost(c->h_counts);
+    for (cudaEvent_t e : c->events) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -728,6 +886,12 @@ int rt_set_counting(void* ctx, int enabled) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return RT_ERR_INVALID_ARG;
     c->counting = enabled != 0;
+    return RT_OK;
+}
+int rt_set_renderer(void* ctx, int mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || mode < RT_RENDERER_AUTO || mode > RT_RENDERER_WAVEFRONT) return RT_ERR_INVALID_ARG;
+    c->renderer = mode;
     return RT_OK;
 }
 int rt_cancel(void* ctx) {

@@ -13,7 +13,7 @@
 
 namespace rtd {
 
-#define NF __device__ __noinline__
+#define NF static __device__ __noinline__
 
 /* the scene services share one traversal context per path */
 struct Ctx {

@@ -1,0 +1,441 @@
+/*
+ * rt_wavefront.cu - wavefront renderer for the `path` integrator.
+ *
+ * The megakernel runs PathTracer.Li (Integrators/PathTracer.cs) as one loop
+ * per thread.  Here the loop is cut at its ray casts and the pieces run as
+ * separate kernels over compacted queues:
+ *
+ *   k_wf_trace   every queued ray (extension closest-hit, shadow any-hit, MIS
+ *                closest-hit) in one lean traversal kernel;
+ *   k_wf_shade   per path: first adds the direct-lighting term scheduled in
+ *                the previous shade (its shadow / MIS rays are now resolved),
+ *                then runs one bounce of the reference loop on the new
+ *                extension hit and enqueues the next rays.
+ *
+ * All random numbers of a bounce are drawn in k_wf_shade in the reference's
+ * order, and the radiance of a path is accumulated in the reference's order
+ * (the deferred direct term of bounce b is added before the emission of
+ * bounce b+1), so every sample is bit-identical to the megakernel and to the
+ * CPU oracle.  Path slots whose path has finished are refilled with the next
+ * camera sample, which keeps the queues full to the end of a render.
+ */
+#include <cuda_runtime.h>
+#include "rt_integrators.cuh"
+#include "rt_wavefront.h"
+
+using namespace rtd;
+
+namespace {
+
+enum : uint32_t {
+    F_ALIVE = 1u,        /* the slot holds a path */
+    F_SPECULAR = 2u,     /* isSpecularPath */
+    F_PENDING = 4u,      /* a direct-lighting term waits for its rays */
+    F_L1 = 8u,           /* pending light-sample term (gated by the shadow ray) */
+    F_L2 = 16u,          /* pending BSDF-sample term (resolved by the MIS ray) */
+    F_DZERO = 32u,       /* pending direct term is exactly zero (no light / no estimate) */
+    F_DONE = 64u,        /* the path ends once its pending term is added */
+    F_EXT = 128u,        /* an extension ray was enqueued */
+};
+
+DF void warp_add64(unsigned long long* dst, uint32_t v) {
+    unsigned mask = __activemask();
+    uint32_t s = __reduce_add_sync(mask, v);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(mask) - 1) && s) atomicAdd(dst, (unsigned long long)s);
+}
+
+/* warp-aggregated append to a queue counter */
+DF int warp_append(int* counter, bool want) {
+    unsigned mask = __ballot_sync(__activemask(), want);
+    if (!want) return -1;
+    int leader = __ffs(mask) - 1;
+    int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
+    W.q_o[q] = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
+    W.q_d[q] = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
+    W.q_meta[q] = (path << 2) | kind;
+}
+
+/* Rng resumed at draw n of its stream */
+DF void rng_resume(Rng& r, uint64_t seed, uint32_t x, uint32_t y, uint32_t s, uint32_t n) {
+    rng_init(r, seed, x, y, s);
+    r.n = n;
+    if (n & 3u) philox(r.c0, r.c1, r.c2, n >> 2, r.k0, r.k1, r.buf);
+}
+
+/* sample id -> crop pixel (8x4 tiles so that neighbouring paths are neighbouring pixels) */
+DF void sample_pixel(const RtParams& P, int64_t sid, int* lx, int* ly, int* k) {
+    const int tw = (P.w + 7) >> 3, th = (P.h + 3) >> 2;
+    const int64_t per = (int64_t)tw * th * 32;
+    *k = (int)(sid / per);
+    int64_t r = sid - (int64_t)(*k) * per;
+    int tile = (int)(r >> 5), lane = (int)(r & 31);
+    *lx = (tile % tw) * 8 + (lane & 7);
+    *ly = (tile / tw) * 4 + (lane >> 3);
+}
+
+/* initialises a camera sample in `slot` and enqueues its first ray; returns false when no sample is left */
+DF bool start_path(const RtSceneView* S, const RtParams& P, const WfState& W, int slot, bool take) {
+    int64_t sid = -1;
+    int lx = 0, ly = 0, k = 0;
+    if (take) {
+        const int tw = (P.w + 7) >> 3, th = (P.h + 3) >> 2;
+        const int64_t total = (int64_t)tw * th * 32 * P.chunk_len;
+        /* skip ids that fall outside the crop (partial tiles) */
+        while (true) {
+            sid = (int64_t)atomicAdd(W.next_sample, 1ull);
+            if (sid >= total) { sid = -1; break; }
+            sample_pixel(P, sid, &lx, &ly, &k);
+            if (lx < P.w && ly < P.h) break;
+        }
+    }
+    int q = warp_append(W.n_rays_next, sid >= 0);
+    if (sid < 0) { W.flags[slot] = 0; return false; }
+    int px = P.x0 + lx, py = P.y0 + ly, t = P.sample_begin + P.chunk_begin + k;
+    Rng rand;
+    rng_init(rand, P.seed, (uint32_t)px, (uint32_t)py, (uint32_t)t);
+    V2 jit = NextVec2(rand);
+    Ray ray = CameraRay(S->camera, v2((float)px + jit.x, (float)py + jit.y));
+    W.pix[slot] = make_int4(lx, ly, k, t);
+    W.rng_n[slot] = rand.n;
+    W.coeff[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    W.rad[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    W.bounce[slot] = make_int2(0, 0);
+    W.flags[slot] = F_ALIVE | F_SPECULAR | F_EXT;
+    W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
+    W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
+    push_ray(W, q, slot, WF_RAY_EXT, ray);
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_wf_start(const RtSceneView* __restrict__ S, RtParams P, WfState W, int slots) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= slots) return;
+    start_path(S, P, W, slot, true);
+}
+
+/* one traversal kernel for every queued ray */
+__global__ void __launch_bounds__(128) k_wf_trace(const RtSceneView* __restrict__ S, WfState W, int n,
+                                                    uint32_t* status, unsigned long long* stats, bool counting) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 o = W.q_o[i], d = W.q_d[i];
+    const int meta = W.q_meta[i];
+    const int path = meta >> 2, kind = meta & 3;
+    Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
+    int2 stack[2 * RT_STACK_SIZE];
+    TravStats st = {0, 0, 0};
+    TravStats* stp = counting ? &st : nullptr;
+    if (kind == WF_RAY_SHADOW) {
+        W.occluded[path] = BvhAny<true>(S, 0, ray, stack, status, stp) ? 1 : 0;
+    } else {
+        Best b;
+        Ray r = ray;
+        bool hit = BvhClosest<true>(S, 0, r, &b, stack, status, stp);
+        float4 h = make_float4(b.t, b.u, b.v, __int_as_float(hit ? b.slot : -1));
+        if (kind == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = b.sub; }
+        else { W.mis_hit[path] = h; W.mis_sub[path] = b.sub; }
+    }
+    if (counting) {
+        warp_add64(stats + (kind == WF_RAY_SHADOW ? 2 : 1), 1u);
+        warp_add64(stats + 3, st.nodes);
+        warp_add64(stats + 4, st.prims);
+        warp_add64(stats + 5, st.insts);
+    }
+}
+
+DF bool load_hit(const RtSceneView* S, const Ray& ray, float4 h, int sub, Isect* it) {
+    int slot = __float_as_int(h.w);
+    if (slot < 0) return false;
+    Best b;
+    b.t = h.x; b.u = h.y; b.v = h.z; b.slot = slot; b.sub = sub; b.flags = 0;
+    b.pw = v3s(0);
+    /* instance hits: the world point is recomputed exactly as during traversal */
+    float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
+    uint32_t kr = __float_as_uint(s1.w);
+    if ((kr >> RT_KIND_SHIFT) == RT_KIND_INSTANCE) {
+        const RtInstance& I = S->instances[kr & RT_REF_MASK];
+        float w2m[12], m2w[12];
+        for (int q = 0; q < 12; q++) { w2m[q] = I.w2m[q]; m2w[q] = I.m2w[q]; }
+        float4 p1 = __ldg(S->slots + 3 * (int64_t)sub + 1);
+        uint32_t pkr = __float_as_uint(p1.w);
+        V3 pm;
+        if ((pkr >> RT_KIND_SHIFT) == RT_KIND_TRI) {
+            V3 bary = v3(1 - (b.u + b.v), b.u, b.v);
+            RtTri t = S->tris[pkr & RT_REF_MASK];
+            pm = bary.x * f4xyz(S->pos[t.v0]) + bary.y * f4xyz(S->pos[t.v1]) + bary.z * f4xyz(S->pos[t.v2]);
+        } else {
+            RtSphere sph = S->spheres[pkr & RT_REF_MASK];
+            V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
+            Ray mr = XfRay(ray, w2m);
+            float tm = 0;
+            SphereTest(c, sph.radius, mr, &tm);
+            V3 n = Normalize(At(mr, tm) - c);
+            pm = n * sph.radius + c;
+        }
+        b.pw = Xf12(pm, m2w);
+    }
+    Finish(S, ray, b, it);
+    return true;
+}
+
+DF void finish_path(const RtParams& P, const WfState& W, int slot, C3 rad, unsigned long long* stats) {
+    bool invalid = !IsValid(rad);
+    if (invalid) { rad = c3s(0.0f); atomicAdd(stats + 6, 1ull); }
+    int4 px = W.pix[slot];
+    const int64_t npix = (int64_t)P.w * P.h;
+    float* o = W.samples + ((int64_t)px.z * npix + (int64_t)px.x * P.h + px.y) * 3;
+    o[0] = rad.r; o[1] = rad.g; o[2] = rad.b;
+}
+
+/* one bounce of PathTracer.Mis / NextEventEstimation / OnlySampleBxdf after the
+ * extension hit is known (PathTracer.cs:43-270) */
+__global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict__ S, RtParams P, WfState W, int n,
+                                                    uint32_t* status, unsigned long long* stats, bool counting,
+                                                    bool regenerate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int slot = W.active[i];
+    uint32_t fl = W.flags[slot];
+    float4 cf = W.coeff[slot], rd = W.rad[slot];
+    C3 coeff = c3(cf.x, cf.y, cf.z), radiance = c3(rd.x, rd.y, rd.z);
+
+    /* 1. the direct term scheduled by the previous bounce */
+    if (fl & F_PENDING) {
+        float4 pc = W.pd_coeff[slot];
+        C3 coeffb = c3(pc.x, pc.y, pc.z);
+        float lightPdf = pc.w;
+        if (P.method == RT_METHOD_MIS) {
+            C3 direct = c3s(0);
+            if (!(fl & F_DZERO)) {
+                C3 le = c3s(0.0f);
+                if ((fl & F_L1) && !W.occluded[slot]) {
+                    float4 l1 = W.pd_l1[slot];
+                    le = le + c3(l1.x, l1.y, l1.z);
+                }
+                if (fl & F_L2) {
+                    float4 fr2 = W.pd_fr[slot];
+                    float4 mi = W.pd_mis[slot];
+                    float4 wl = W.pd_w[slot];
+                    const int light = __float_as_int(mi.y);
+                    C3 li = c3s(0);
+                    Isect lit;
+                    float4 mo = W.pd_ray_o[slot], md = W.pd_ray_d[slot];
+                    Ray mr = mkray(v3(mo.x, mo.y, mo.z), v3(md.x, md.y, md.z), mo.w, md.w);
+                    if (load_hit(S, mr, W.mis_hit[slot], W.mis_sub[slot], &lit)) {
+                        if (LightOf(S, lit) >= 0 && LightOf(S, lit) == light) li = IsectLe(S, lit, v3(wl.x, wl.y, wl.z));
+                    } else {
+                        li = EvalAllInfinite(S, mr.D);
+                    }
+                    if (!IsBlack(li)) le = le + c3(fr2.x, fr2.y, fr2.z) * li * fr2.w / mi.x;
+                }
+                direct = direct + le / lightPdf;
+            }
+            radiance = radiance + coeffb * direct;
+        } else { /* NEE */
+            C3 e = c3s(0);
+            if (!(fl & F_DZERO) && !W.occluded[slot]) { float4 l1 = W.pd_l1[slot]; e = c3(l1.x, l1.y, l1.z); }
+            radiance = radiance + coeffb * e / lightPdf;
+        }
+        fl &= ~(F_PENDING | F_L1 | F_L2 | F_DZERO);
+    }
+
+    bool done = (fl & F_DONE) != 0;
+    if (!done) {
+        /* 2. the bounce itself */
+        int2 bc = W.bounce[slot];
+        int bounces = bc.x, guard = bc.y;
+        float4 ro = W.ray_o[slot], rdd = W.ray_d[slot];
+        Ray ray = mkray(v3(ro.x, ro.y, ro.z), v3(rdd.x, rdd.y, rdd.z), ro.w, rdd.w);
+        int4 px = W.pix[slot];
+        Rng rand;
+        rng_resume(rand, P.seed, (uint32_t)(P.x0 + px.x), (uint32_t)(P.y0 + px.y), (uint32_t)px.w, W.rng_n[slot]);
+        bool isSpecularPath = (fl & F_SPECULAR) != 0;
+        Ray nray = ray;
+        bool ext = false;
+        do {
+            if (++guard > RT_LOOP_CAP) { atomicOr(status, RT_STATUS_ITER); done = true; break; }
+            Isect it;
+            bool isHit = load_hit(S, ray, W.ext_hit[slot], W.ext_sub[slot], &it);
+            V3 wo = -ray.D;
+            if (P.method == RT_METHOD_BXDF) {
+                if (!isHit) { radiance = radiance + coeff * EvalAllInfinite(S, ray.D); done = true; break; }
+                if (P.max_depth != -1 && bounces >= P.max_depth) { done = true; break; }
+                if (!HasSurface(S, it)) { nray = mkray(it.P, ray.D, ray.MinT); ext = true; break; }
+                if (LightOf(S, it) >= 0) radiance = radiance + coeff * IsectLe(S, it, wo);
+            } else {
+                if (bounces == 0 || isSpecularPath) {
+                    if (isHit) radiance = radiance + coeff * IsectLe(S, it, wo);
+                    else radiance = radiance + coeff * EvalAllInfinite(S, ray.D);
+                }
+                if (!isHit) { done = true; break; }
+                if (P.max_depth != -1 && bounces >= P.max_depth) { done = true; break; }
+                if (!HasSurface(S, it)) { nray = mkray(it.P, ray.D, ray.MinT); ext = true; break; }
+                /* direct lighting: everything but the two ray casts */
+                const int mat = PrimOf(S, it).material;
+                int light;
+                float lightPdf = SampleLight(S, rand, &light);
+                if (P.method == RT_METHOD_MIS) {
+                    fl |= F_PENDING;
+                    W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+                    if (lightPdf > 0.0f) {
+                        V3 wod = it.Wr;
+                        LSample ls = LightSampleLi(S, light, it.P, rand);
+                        if (ls.Pdf > 0.0f && !IsBlack(ls.Li)) {
+                            C3 fr = MatFr(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                            float scatteringPdf = MatPdf(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                            if (!IsBlack(fr)) {
+                                /* IsOccluded(it.P, ls.P) */
+                                V3 vec = ls.P - it.P;
+                                float dis = Length(vec);
+                                if (!(dis < 0.001f)) {
+                                    fr = fr * AbsCosTheta(Lo(it, ls.Wi));
+                                    float weight = PowerHeuristic(ls.Pdf, scatteringPdf);
+                                    C3 l1 = fr * ls.Li * weight / ls.Pdf;
+                                    W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
+                                    fl |= F_L1;
+                                    int q = warp_append(W.n_rays_next, true);
+                                    push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
+                                }
+                            }
+                        }
+                        BSample sample = MatSample(S, mat, Lo(it, wod), it.UV, rand);
+                        C3 fr = sample.Fr * AbsCosTheta(sample.Wi);
+                        float scatteringPdf = sample.Pdf;
+                        bool sampledSpecular = (sample.Type & BX_SPECULAR) != 0;
+                        if (!IsBlack(fr) && scatteringPdf > 0) {
+                            float weight = 1;
+                            bool go = true;
+                            if (!sampledSpecular) {
+                                float bxdfToLightPdf = LightPdfLi(S, light, it.P, Wo(it, sample.Wi));
+                                if (bxdfToLightPdf == 0.0f) go = false;
+                                else weight = PowerHeuristic(scatteringPdf, bxdfToLightPdf);
+                            }
+                            if (go) {
+                                Ray toLight = Spawn(it, Wo(it, sample.Wi));
+                                V3 wle = Wo(it, -sample.Wi);
+                                W.pd_fr[slot] = make_float4(fr.r, fr.g, fr.b, weight);
+                                W.pd_mis[slot] = make_float4(scatteringPdf, __int_as_float(light), 0, 0);
+                                W.pd_w[slot] = make_float4(wle.x, wle.y, wle.z, 0);
+                                W.pd_ray_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
+                                W.pd_ray_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, toLight.MaxT);
+                                fl |= F_L2;
+                                int q = warp_append(W.n_rays_next, true);
+                                push_ray(W, q, slot, WF_RAY_MIS, toLight);
+                            }
+                        }
+                    } else {
+                        fl |= F_DZERO;
+                    }
+                } else { /* NEE: NeeEstimateLight */
+                    if (lightPdf > 0.0f) {
+                        fl |= F_PENDING;
+                        W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+                        LSample r = LightSampleLi(S, light, it.P, rand);
+                        bool zero = true;
+                        if (r.Pdf > 0.0f) {
+                            V3 vec = r.P - it.P;
+                            float dis = Length(vec);
+                            if (!(dis < 0.001f)) {
+                                C3 fr = MatFr(S, mat, Lo(it, wo), Lo(it, r.Wi), it.UV);
+                                C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
+                                W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
+                                zero = false;
+                                int q = warp_append(W.n_rays_next, true);
+                                push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
+                            }
+                        }
+                        if (zero) fl |= F_DZERO;
+                    }
+                }
+            }
+            /* continuation */
+            BSample s = MatSample(S, PrimOf(S, it).material, Lo(it, wo), it.UV, rand);
+            if (P.method != RT_METHOD_BXDF) isSpecularPath = (s.Type & BX_SPECULAR) != 0;
+            if (s.Pdf > 0.0f) coeff = coeff * (s.Fr * AbsCosTheta(s.Wi) / s.Pdf);
+            else { done = true; break; }
+            nray = Spawn(it, Wo(it, s.Wi));
+            if (bounces > P.min_depth) {
+                float q = nmin(MaxElement(coeff), P.rr);
+                if (NextFloat(rand) > q) { done = true; break; }
+                coeff = coeff / q;
+            }
+            bounces++;
+            ext = true;
+        } while (false);
+        if (ext) {
+            int q = warp_append(W.n_rays_next, true);
+            push_ray(W, q, slot, WF_RAY_EXT, nray);
+            W.ray_o[slot] = make_float4(nray.O.x, nray.O.y, nray.O.z, nray.MinT);
+            W.ray_d[slot] = make_float4(nray.D.x, nray.D.y, nray.D.z, nray.MaxT);
+        }
+        W.bounce[slot] = make_int2(bounces, guard);
+        W.rng_n[slot] = rand.n;
+        fl = (fl & ~F_SPECULAR) | (isSpecularPath ? F_SPECULAR : 0u);
+        if (done) fl |= F_DONE;
+    }
+    W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0);
+    W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0);
+    /* the slot stays active while it waits for rays */
+    if (fl & F_PENDING) {
+        W.flags[slot] = fl;
+        int a = warp_append(W.n_active_next, true);
+        W.active_next[a] = slot;
+        return;
+    }
+    if (!(fl & F_DONE)) {
+        W.flags[slot] = fl;
+        int a = warp_append(W.n_active_next, true);
+        W.active_next[a] = slot;
+        return;
+    }
+    finish_path(P, W, slot, radiance, stats);
+    if (counting) warp_add64(stats + 0, 1u);
+    if (regenerate && start_path(S, P, W, slot, true)) {
+        int a = warp_append(W.n_active_next, true);
+        W.active_next[a] = slot;
+    } else {
+        W.flags[slot] = 0;
+        warp_append(W.n_active_next, false);
+    }
+}
+
+__global__ void k_wf_active_init(WfState W, int slots) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= slots) return;
+    bool alive = (W.flags[i] & F_ALIVE) != 0;
+    int a = warp_append(W.n_active, alive);
+    if (alive) W.active[a] = i;
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& W, int slots, cudaStream_t s) {
+    k_wf_start<<<grid_for(slots, 256), 256, 0, s>>>(S, P, W, slots);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_wf_active_init<<<grid_for(slots, 256), 256, 0, s>>>(W, slots);
+    return cudaGetLastError();
+}
+
+cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n, uint32_t* status, unsigned long long* stats,
+                        bool counting, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_wf_trace<<<grid_for(n, 128), 128, 0, s>>>(S, W, n, status, stats, counting);
+    return cudaGetLastError();
+}
+
+cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
+                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(S, P, W, n, status, stats, counting, regenerate);
+    return cudaGetLastError();
+}

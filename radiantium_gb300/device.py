@@ -60,6 +60,10 @@ class Device:
     def set_counting(self, on: bool):
         self._check(self.lib.rt_set_counting(self.h, 1 if on else 0))
 
+    def set_renderer(self, mode: int):
+        """N.RENDERER_AUTO / RENDERER_MEGAKERNEL / RENDERER_WAVEFRONT"""
+        self._check(self.lib.rt_set_renderer(self.h, mode))
+
     def stats(self) -> dict:
         st = N.Stats()
         self._check(self.lib.rt_get_stats(self.h, C.byref(st)))

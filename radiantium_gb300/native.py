@@ -106,10 +106,14 @@ class RenderParams(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64),
                 ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64), ("instance_visits", C.c_uint64),
-                ("invalid_samples", C.c_uint64), ("reserved", C.c_uint64 * 5)]
+                ("invalid_samples", C.c_uint64), ("kernel_launches", C.c_uint64), ("render_launches", C.c_uint64),
+                ("render_kernel_ms", C.c_double), ("shade_kernel_ms", C.c_double), ("reserved", C.c_uint64 * 1)]
 
     def as_dict(self):
-        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k not in ("reserved", "render_kernel_ms", "shade_kernel_ms")}
+        d["render_kernel_ms"] = float(self.render_kernel_ms)
+        d["shade_kernel_ms"] = float(self.shade_kernel_ms)
+        return d
 
 
 # numpy structured dtypes with the same layout (rays/hits are passed as arrays)
@@ -130,8 +134,9 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_get_stats", "rt_set_counting", "rt_cancel",
+    "rt_render", "rt_render_device", "rt_get_stats", "rt_set_counting", "rt_set_renderer", "rt_cancel",
 ]
+RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT = 0, 1, 2
 
 _lib = None
 
@@ -164,6 +169,8 @@ def _declare(lib):
     lib.rt_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.rt_set_counting.restype = C.c_int
     lib.rt_set_counting.argtypes = [vp, C.c_int]
+    lib.rt_set_renderer.restype = C.c_int
+    lib.rt_set_renderer.argtypes = [vp, C.c_int]
     lib.rt_cancel.restype = C.c_int
     lib.rt_cancel.argtypes = [vp]
     return lib

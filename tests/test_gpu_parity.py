@@ -117,24 +117,52 @@ def test_camera_rays_trace(dev, cornell):
     assert_hits_equal(dev.trace_closest(rays), orc.trace_closest(rays))
 
 
+RENDERERS = [N.RENDERER_MEGAKERNEL, N.RENDERER_WAVEFRONT]
+
+
+def _render(dev, st, renderer):
+    dev.set_renderer(renderer)
+    try:
+        return dev.render(st)
+    finally:
+        dev.set_renderer(N.RENDERER_AUTO)
+
+
+@pytest.mark.parametrize("renderer", RENDERERS)
 @pytest.mark.parametrize("method", [N.METHOD_MIS, N.METHOD_NEE, N.METHOD_BXDF])
 @pytest.mark.parametrize("strategy", [N.STRATEGY_UNIFORM, N.STRATEGY_ALL])
-def test_render_cornell_bitexact(dev, cornell, method, strategy):
+def test_render_cornell_bitexact(dev, cornell, method, strategy, renderer):
     s, st, orc = cornell
+    if renderer == N.RENDERER_WAVEFRONT and strategy == N.STRATEGY_ALL:
+        pytest.skip("the wavefront renderer runs the Uniform light strategy")
     dev.upload(s)
     st = st.replace(spp=3, method=method, strategy=strategy)
-    g, o = dev.render(st), orc.render(st)
+    g, o = _render(dev, st, renderer), orc.render(st)
     assert g.shape == (64, 64, 3)
     assert np.array_equal(_bits(g), _bits(o)), f"max abs diff {np.abs(g - o).max()}"
 
 
+@pytest.mark.parametrize("renderer", RENDERERS)
 @pytest.mark.parametrize("method", [N.METHOD_MIS, N.METHOD_NEE, N.METHOD_BXDF])
-def test_render_materials_bitexact(dev, zoo, method):
+def test_render_materials_bitexact(dev, zoo, method, renderer):
     s, st, orc = zoo
     dev.upload(s)
     st = st.replace(method=method)
-    g, o = dev.render(st), orc.render(st)
+    g, o = _render(dev, st, renderer), orc.render(st)
     assert np.array_equal(_bits(g), _bits(o)), f"max abs diff {np.abs(g - o).max()}"
+
+
+def test_wavefront_matches_megakernel_large(dev):
+    """Many regenerated path slots: 96x96 x 16 spp of the instanced-sphere scene."""
+    from radiantium_gb300 import procedural as P
+    s, st = P.instanced_spheres(96, 96, sphere_n=12, grid=4, env_w=64, env_h=32)
+    dev.upload(s)
+    st = st.replace(spp=16)
+    a = _render(dev, st, N.RENDERER_MEGAKERNEL)
+    b = _render(dev, st, N.RENDERER_WAVEFRONT)
+    assert np.array_equal(_bits(a), _bits(b)), f"max abs diff {np.abs(a - b).max()}"
+    o = OracleScene(s).render(st.replace(x0=20, y0=30, width=24, height=16))
+    assert np.array_equal(_bits(b[20:44, 30:46]), _bits(o))
 
 
 def test_render_volume_bitexact(dev):
@@ -158,12 +186,13 @@ def test_render_crop_and_resume(dev, cornell):
     assert np.array_equal(_bits(later), _bits(orc.render(st.replace(spp=2, sample_begin=2))))
 
 
-def test_counters_match_oracle(dev, cornell):
+@pytest.mark.parametrize("renderer", RENDERERS)
+def test_counters_match_oracle(dev, cornell, renderer):
     s, st, orc = cornell
     dev.upload(s)
     dev.set_counting(True)
     st = st.replace(spp=2)
-    dev.render(st)
+    _render(dev, st, renderer)
     g = dev.stats()
     dev.set_counting(False)
     _, o = orc.render(st, stats=True)
