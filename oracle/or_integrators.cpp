@@ -527,6 +527,10 @@ int or_detmath(int fn, const float* a, const float* b, float* out, int64_t n) {
     }
     return RT_OK;
 }
+int or_philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+    Philox4x32(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1], out);
+    return RT_OK;
+}
 int or_philox(uint64_t seed, uint32_t x, uint32_t y, uint32_t s, int count, uint32_t* out) {
     Rng r(seed, x, y, s);
     for (int i = 0; i < count; i++) out[i] = r.NextU32();

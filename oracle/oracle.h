@@ -39,6 +39,7 @@ int or_bvh(void* s, int which, int64_t* node_count, int64_t* prim_count,
 
 /* deterministic math and RNG known-answer hooks */
 int or_detmath(int fn, const float* a, const float* b, float* out, int64_t n);
+int or_philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 int or_philox(uint64_t seed, uint32_t x, uint32_t y, uint32_t s, int count, uint32_t* out);
 
 #ifdef __cplusplus

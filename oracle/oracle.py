@@ -43,6 +43,7 @@ def lib():
         L.or_bvh.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp, vp, vp, vp, vp]
         L.or_detmath.argtypes = [C.c_int, vp, vp, vp, C.c_int64]
         L.or_philox.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, vp]
+        L.or_philox_raw.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -145,4 +146,12 @@ def detmath(fn: str, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:
 def philox_stream(seed: int, x: int, y: int, s: int, count: int) -> np.ndarray:
     out = np.zeros(count, dtype=np.uint32)
     lib().or_philox(seed, x, y, s, count, _ptr(out))
+    return out
+
+
+def philox_raw(ctr, key) -> np.ndarray:
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().or_philox_raw(_ptr(c), _ptr(k), _ptr(out))
     return out

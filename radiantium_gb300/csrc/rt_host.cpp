@@ -901,6 +901,32 @@ int rt_cancel(void* ctx) {
     return RT_OK;
 }
 
+/* test hook (not part of radiantium.h): builds the SAH tree of n primitive
+ * boxes (6 floats each) on the host exactly as rt_upload_scene does and
+ * returns it in depth-first LinearBVHNode form.  Call with null arrays to get
+ * the node count.  No CUDA call is made. */
+int rt_debug_bvh(const float* boxes, int n, int max_prims, int64_t* node_count, float* bounds, int32_t* idx,
+                 int32_t* count, int32_t* axis, int32_t* order) {
+    if (!boxes || n <= 0 || !node_count) return RT_ERR_INVALID_ARG;
+    try {
+        std::vector<rtb::Box> b(n);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) { b[i].mn[k] = boxes[6 * i + k]; b[i].mx[k] = boxes[6 * i + 3 + k]; }
+        rtb::BuildResult r = rtb::build_sah(b, max_prims, std::max(1u, std::thread::hardware_concurrency()));
+        *node_count = (int64_t)r.nodes.size();
+        if (bounds) {
+            for (size_t i = 0; i < r.nodes.size(); i++) {
+                for (int k = 0; k < 3; k++) { bounds[6 * i + k] = r.nodes[i].bounds.mn[k]; bounds[6 * i + 3 + k] = r.nodes[i].bounds.mx[k]; }
+                idx[i] = r.nodes[i].second; count[i] = r.nodes[i].count; axis[i] = r.nodes[i].axis;
+            }
+            for (int i = 0; i < n; i++) order[i] = r.order[i];
+        }
+        return RT_OK;
+    } catch (...) {
+        return RT_ERR_OOM;
+    }
+}
+
 /* test hook (not part of radiantium.h): runs rt_detmath (fn 0..7) or CUDA's
  * own functions (fn 100..107) on the device over host arrays */
 int rt_debug_detmath(void* ctx, int fn, const float* a, const float* b, float* out, int64_t n) {
