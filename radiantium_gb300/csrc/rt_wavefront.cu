@@ -69,34 +69,39 @@ DF void rng_resume(Rng& r, uint64_t seed, uint32_t x, uint32_t y, uint32_t s, ui
     if (n & 3u) philox(r.c0, r.c1, r.c2, n >> 2, r.k0, r.k1, r.buf);
 }
 
-/* sample id -> crop pixel (8x4 tiles so that neighbouring paths are neighbouring pixels) */
+/* sample id -> (crop pixel, sample index in chunk): ids are dense over the
+ * crop; within a sample index the pixels run through bands of four rows,
+ * column by column, so 32 consecutive ids cover an 8x4 pixel tile */
 DF void sample_pixel(const RtParams& P, int64_t sid, int* lx, int* ly, int* k) {
-    const int tw = (P.w + 7) >> 3, th = (P.h + 3) >> 2;
-    const int64_t per = (int64_t)tw * th * 32;
-    *k = (int)(sid / per);
-    int64_t r = sid - (int64_t)(*k) * per;
-    int tile = (int)(r >> 5), lane = (int)(r & 31);
-    *lx = (tile % tw) * 8 + (lane & 7);
-    *ly = (tile / tw) * 4 + (lane >> 3);
+    const int64_t npix = (int64_t)P.w * P.h;
+    *k = (int)(sid / npix);
+    const int r = (int)(sid - (int64_t)(*k) * npix);
+    const int band = r / (4 * P.w);
+    const int bh = min(4, P.h - band * 4);
+    const int rr = r - band * 4 * P.w;
+    *lx = rr / bh;
+    *ly = band * 4 + rr % bh;
 }
 
-/* initialises a camera sample in `slot` and enqueues its first ray; returns false when no sample is left */
+/* initialises a camera sample in `slot` and enqueues its first ray; the
+ * warp claims its sample ids with one atomic.  Returns false (slot emptied)
+ * when every sample of the chunk has been started. */
 DF bool start_path(const RtSceneView* S, const RtParams& P, const WfState& W, int slot, bool take) {
+    const int64_t total = (int64_t)P.w * P.h * P.chunk_len;
+    unsigned mask = __ballot_sync(__activemask(), take);
     int64_t sid = -1;
-    int lx = 0, ly = 0, k = 0;
     if (take) {
-        const int tw = (P.w + 7) >> 3, th = (P.h + 3) >> 2;
-        const int64_t total = (int64_t)tw * th * 32 * P.chunk_len;
-        /* skip ids that fall outside the crop (partial tiles) */
-        while (true) {
-            sid = (int64_t)atomicAdd(W.next_sample, 1ull);
-            if (sid >= total) { sid = -1; break; }
-            sample_pixel(P, sid, &lx, &ly, &k);
-            if (lx < P.w && ly < P.h) break;
-        }
+        int leader = __ffs(mask) - 1, lane = threadIdx.x & 31;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(W.next_sample, (unsigned long long)__popc(mask));
+        base = __shfl_sync(mask, base, leader);
+        int64_t id = (int64_t)base + __popc(mask & ((1u << lane) - 1u));
+        if (id < total) sid = id;
     }
     int q = warp_append(W.n_rays_next, sid >= 0);
     if (sid < 0) { W.flags[slot] = 0; return false; }
+    int lx, ly, k;
+    sample_pixel(P, sid, &lx, &ly, &k);
     int px = P.x0 + lx, py = P.y0 + ly, t = P.sample_begin + P.chunk_begin + k;
     Rng rand;
     rng_init(rand, P.seed, (uint32_t)px, (uint32_t)py, (uint32_t)t);
