@@ -702,6 +702,8 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     WfState W = c->wf;
     W.samples = c->samples;
     W.n_rays_next = c->wf_counters;
+    W.n_shadow_next = c->wf_counters + 3;
+    W.shadow_base = 2 * slots;
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
     for (int b = 0; b < P.spp; b += chunk) {
@@ -716,26 +718,28 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
         CK(cudaMemsetAsync(W.next_sample, 0, sizeof(unsigned long long), s));
         CK(rt_wf_start(c->d_view, P, W, slots, s));
         launches += 2;
-        CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        int n_rays = c->h_counts[0], n_active = c->h_counts[1];
+        int n_rays = c->h_counts[0], n_active = c->h_counts[1], n_shadow = c->h_counts[3];
         while (n_active > 0) {
             if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
             CK(cudaEventRecord(c->events[0], s));
-            CK(rt_wf_trace(c->d_view, W, n_rays, c->status, c->stats, c->counting, s));
+            CK(rt_wf_trace(c->d_view, W, n_rays, n_shadow, c->status, c->stats, c->counting, s));
             CK(cudaEventRecord(c->events[1], s));
             CK(cudaMemsetAsync(W.n_rays_next, 0, sizeof(int32_t), s));
+            CK(cudaMemsetAsync(W.n_shadow_next, 0, sizeof(int32_t), s));
             CK(cudaMemsetAsync(W.n_active_next, 0, sizeof(int32_t), s));
             CK(cudaEventRecord(c->events[2], s));
             CK(rt_wf_shade(c->d_view, P, W, n_active, c->status, c->stats, c->counting, true, s));
             CK(cudaEventRecord(c->events[3], s));
-            launches += (n_rays > 0 ? 1 : 0) + 1;
-            trace_launches += n_rays > 0 ? 1 : 0;
+            launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0) + 1;
+            trace_launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0);
             std::swap(W.active, W.active_next);
             std::swap(W.n_active, W.n_active_next);
-            CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             n_rays = c->h_counts[0];
+            n_shadow = c->h_counts[3];
             n_active = c->h_counts[W.n_active - c->wf_counters];
             float t = 0;
             CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;

@@ -5,8 +5,9 @@
  * per thread.  Here the loop is cut at its ray casts and the pieces run as
  * separate kernels over compacted queues:
  *
- *   k_wf_trace   every queued ray (extension closest-hit, shadow any-hit, MIS
- *                closest-hit) in one lean traversal kernel;
+ *   k_wf_trace_closest / k_wf_trace_shadow   the queued rays: extension and
+ *                MIS rays (closest hit), shadow rays (any hit), each kind in
+ *                its own kernel so the two traversal loops never share a warp;
  *   k_wf_shade   per path: first adds the direct-lighting term scheduled in
  *                the previous shade (its shadow / MIS rays are now resolved),
  *                then runs one bounce of the reference loop on the new
@@ -125,9 +126,9 @@ __global__ void __launch_bounds__(256) k_wf_start(const RtSceneView* __restrict_
     start_path(S, P, W, slot, true);
 }
 
-/* one traversal kernel for every queued ray */
-__global__ void __launch_bounds__(128) k_wf_trace(const RtSceneView* __restrict__ S, WfState W, int n,
-                                                    uint32_t* status, unsigned long long* stats, bool counting) {
+/* closest-hit rays: extension and MIS rays (queue [0, n)) */
+__global__ void __launch_bounds__(128) k_wf_trace_closest(const RtSceneView* __restrict__ S, WfState W, int n,
+                                                            uint32_t* status, unsigned long long* stats, bool counting) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 o = W.q_o[i], d = W.q_d[i];
@@ -136,19 +137,33 @@ __global__ void __launch_bounds__(128) k_wf_trace(const RtSceneView* __restrict_
     Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
-    TravStats* stp = counting ? &st : nullptr;
-    if (kind == WF_RAY_SHADOW) {
-        W.occluded[path] = BvhAny<true>(S, 0, ray, stack, status, stp) ? 1 : 0;
-    } else {
-        Best b;
-        Ray r = ray;
-        bool hit = BvhClosest<true>(S, 0, r, &b, stack, status, stp);
-        float4 h = make_float4(b.t, b.u, b.v, __int_as_float(hit ? b.slot : -1));
-        if (kind == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = b.sub; }
-        else { W.mis_hit[path] = h; W.mis_sub[path] = b.sub; }
-    }
+    Best b;
+    bool hit = BvhClosest<true>(S, 0, ray, &b, stack, status, counting ? &st : nullptr);
+    float4 h = make_float4(b.t, b.u, b.v, __int_as_float(hit ? b.slot : -1));
+    if (kind == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = b.sub; }
+    else { W.mis_hit[path] = h; W.mis_sub[path] = b.sub; }
     if (counting) {
-        warp_add64(stats + (kind == WF_RAY_SHADOW ? 2 : 1), 1u);
+        warp_add64(stats + 1, 1u);
+        warp_add64(stats + 3, st.nodes);
+        warp_add64(stats + 4, st.prims);
+        warp_add64(stats + 5, st.insts);
+    }
+}
+
+/* shadow rays: any-hit (queue [shadow_base, shadow_base + n)) */
+__global__ void __launch_bounds__(128) k_wf_trace_shadow(const RtSceneView* __restrict__ S, WfState W, int n,
+                                                           uint32_t* status, unsigned long long* stats, bool counting) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int q = W.shadow_base + i;
+    const float4 o = W.q_o[q], d = W.q_d[q];
+    const int path = W.q_meta[q] >> 2;
+    Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
+    int2 stack[2 * RT_STACK_SIZE];
+    TravStats st = {0, 0, 0};
+    W.occluded[path] = BvhAny<true>(S, 0, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
+    if (counting) {
+        warp_add64(stats + 2, 1u);
         warp_add64(stats + 3, st.nodes);
         warp_add64(stats + 4, st.prims);
         warp_add64(stats + 5, st.insts);
@@ -305,7 +320,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
                                     C3 l1 = fr * ls.Li * weight / ls.Pdf;
                                     W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
                                     fl |= F_L1;
-                                    int q = warp_append(W.n_rays_next, true);
+                                    int q = W.shadow_base + warp_append(W.n_shadow_next, true);
                                     push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
                                 }
                             }
@@ -352,7 +367,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
                                 C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
                                 W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
                                 zero = false;
-                                int q = warp_append(W.n_rays_next, true);
+                                int q = W.shadow_base + warp_append(W.n_shadow_next, true);
                                 push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
                             }
                         }
@@ -431,10 +446,12 @@ cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& 
     return cudaGetLastError();
 }
 
-cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n, uint32_t* status, unsigned long long* stats,
-                        bool counting, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_wf_trace<<<grid_for(n, 128), 128, 0, s>>>(S, W, n, status, stats, counting);
+cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
+                        unsigned long long* stats, bool counting, cudaStream_t s) {
+    if (n_closest > 0) k_wf_trace_closest<<<grid_for(n_closest, 128), 128, 0, s>>>(S, W, n_closest, status, stats, counting);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (n_shadow > 0) k_wf_trace_shadow<<<grid_for(n_shadow, 128), 128, 0, s>>>(S, W, n_shadow, status, stats, counting);
     return cudaGetLastError();
 }
 

@@ -12,9 +12,13 @@ enum { WF_RAY_EXT = 0, WF_RAY_SHADOW = 1, WF_RAY_MIS = 2 };
 /* structure-of-arrays path state; every array has one entry per path slot
  * except the ray queue (3 entries per slot) */
 struct WfState {
-    /* ray queue: origin + MinT, direction + MaxT, (slot << 2) | kind */
+    /* ray queue: origin + MinT, direction + MaxT, (slot << 2) | kind.
+     * Closest-hit rays (extension, MIS) fill [0, 2 * slots), shadow rays
+     * [shadow_base, shadow_base + slots): the two ray kinds never share a warp. */
     float4* q_o; float4* q_d; int32_t* q_meta;
     int32_t* n_rays_next;
+    int32_t* n_shadow_next;
+    int32_t shadow_base;
     /* active slot lists (read by the shade kernel / written for the next one) */
     int32_t* active; int32_t* active_next;
     int32_t* n_active; int32_t* n_active_next;
@@ -41,8 +45,8 @@ struct WfState {
 };
 
 cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& W, int slots, cudaStream_t s);
-cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n, uint32_t* status, unsigned long long* stats,
-                        bool counting, cudaStream_t s);
+cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
+                        unsigned long long* stats, bool counting, cudaStream_t s);
 cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
                         unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s);
 
