@@ -274,6 +274,25 @@ int rt_render(void* ctx, const rt_render_params* params, float* out_rgb);
 /* Same, film written to device memory on `stream` (no host copies). */
 int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream);
 
+/* Size of the fixed device scratch behind rt_render_device_noalloc. */
+#define RT_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* rt_render_device without any device allocation.  No counterpart in the
+ * reference: it exists for hosts that cannot let a library allocate device
+ * memory while they render (an engine whose pool allocator owns the whole
+ * GPU, a frame loop that cannot take cudaFree's device-wide synchronisation).
+ * It always runs the megakernel renderer, whatever rt_set_renderer chose, out
+ * of one static device array of RT_NOALLOC_SCRATCH_BYTES.  The first call on
+ * a device sets that array up (the runtime loads its module and reserves it),
+ * so make one call before any stream capture or allocation-free phase begins.
+ * The film sums and one sample plane must fit:
+ * 512 + 2 * 12 * width * height <= RT_NOALLOC_SCRATCH_BYTES (crop size; a
+ * 1024 x 1024 crop fits), else RT_ERR_INVALID_ARG.  Counters are not
+ * gathered.  Every context on a device shares that one array, so calls that
+ * overlap in time on one device race and must be serialised by the caller.
+ * The film is the same as rt_render_device's, bit for bit. */
+int rt_render_device_noalloc(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream);
+
 /* Counters of the last render / trace call (Stopwatch/Logger counterpart). */
 int rt_get_stats(void* ctx, rt_stats* out);
 

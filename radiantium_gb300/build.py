@@ -1,9 +1,11 @@
 """Builds libradiantium_gb300.so in-tree for sm_103a.
 
-Three translation units compiled in parallel and linked with nvcc:
-  rt_kernels.cu  device code: --fmad=false keeps every multiply and add
-                 separately rounded (the reference's arithmetic), IEEE
-                 division and square root are nvcc's defaults;
+Translation units compiled in parallel and linked with nvcc:
+  rt_kernels.cu, rt_wavefront.cu  device code: --fmad=false keeps every
+                 multiply and add separately rounded (the reference's
+                 arithmetic), IEEE division and square root are nvcc's
+                 defaults;
+  rt_noalloc.cu  the fixed scratch array of the allocation-free render;
   rt_host.cpp, rt_bvh.cpp  host runtime and BVH builder, -ffp-contract=off
                  for the same reason.
 """
@@ -40,6 +42,8 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
                          "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_kernels.cu")],
         "rt_wavefront.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                             "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_wavefront.cu")],
+        "rt_noalloc.o": [nvcc, ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *extra_nvcc,
+                         "-c", os.path.join(CSRC, "rt_noalloc.cu")],
         "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                       f"-I{cuda}/include", "-c", os.path.join(CSRC, "rt_host.cpp")],
         "rt_bvh.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",

@@ -64,6 +64,7 @@ struct Ctx {
     float* samples = nullptr; size_t samples_bytes = 0;
     float* film = nullptr; size_t film_bytes = 0;
     float* out = nullptr; size_t out_bytes = 0;
+    unsigned char* noalloc = nullptr;          /* this device's fixed scratch (rt_noalloc.cu) */
     uint32_t* status = nullptr;
     unsigned long long* stats = nullptr;
     void* io = nullptr; size_t io_bytes = 0;   /* device staging for host-pointer calls */
@@ -692,6 +693,66 @@ void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t
     c->last.kernel_launches = launches;
 }
 
+/* rt_render_device_noalloc: the megakernel render with every buffer carved
+ * out of the fixed scratch array.  The first call on a device looks the array
+ * up (which loads its module); after that a call issues only kernels,
+ * memsets, one 4-byte read of the status word and a stream synchronisation,
+ * and allocates nothing. */
+void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t user) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (!c->noalloc) CK(rt_noalloc_scratch(c->device, (void**)&c->noalloc));
+    if (!p || !dst || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render: null params/output or spp <= 0");
+    if (p->integrator != RT_INTEGRATOR_PATH && p->integrator != RT_INTEGRATOR_VOL_PATH) throw RtFail(RT_ERR_INVALID_ARG, "render: unknown integrator");
+    RtParams P{};
+    P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
+    P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;
+    P.seed = p->seed; P.x0 = p->x0; P.y0 = p->y0;
+    P.w = p->width > 0 ? p->width : c->width - p->x0;
+    P.h = p->height > 0 ? p->height : c->height - p->y0;
+    if (P.x0 < 0 || P.y0 < 0 || P.w <= 0 || P.h <= 0 || P.x0 + P.w > c->width || P.y0 + P.h > c->height)
+        throw RtFail(RT_ERR_INVALID_ARG, "render: crop outside the film");
+    P.spp = p->spp; P.sample_begin = p->sample_begin;
+    const int64_t npix = (int64_t)P.w * P.h;
+    const int64_t plane = npix * 12, head = 512, film_bytes = (plane + 255) / 256 * 256;
+    const int64_t room = (int64_t)RT_NOALLOC_SCRATCH_BYTES - head - film_bytes;
+    if (room < plane) {
+        char msg[192];
+        std::snprintf(msg, sizeof(msg), "render_noalloc: a %d x %d crop needs %lld bytes of scratch, the fixed array holds %u",
+                      P.w, P.h, (long long)(head + film_bytes + plane), RT_NOALLOC_SCRATCH_BYTES);
+        throw RtFail(RT_ERR_INVALID_ARG, msg);
+    }
+    uint32_t* status = (uint32_t*)c->noalloc;
+    unsigned long long* stats = (unsigned long long*)(c->noalloc + 256);
+    float* film = (float*)(c->noalloc + head);
+    float* samples = (float*)(c->noalloc + head + film_bytes);
+    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(P.spp, room / plane));
+    cudaStream_t s = user ? user : c->stream;
+    CK(cudaMemsetAsync(c->noalloc, 0, (size_t)head, s));
+    CK(cudaMemsetAsync(film, 0, (size_t)plane, s));
+    c->cancel.store(0);
+    uint64_t launches = 0, chunks = 0;
+    for (int b = 0; b < P.spp; b += chunk) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        P.chunk_begin = b;
+        P.chunk_len = std::min(chunk, P.spp - b);
+        CK(rt_launch_render(c->d_view, P, samples, status, stats, false, s));
+        CK(rt_launch_accumulate(film, samples, npix, P.chunk_len, s));
+        launches += 2;
+        chunks++;
+    }
+    CK(rt_launch_finalize(dst, film, npix, (float)P.spp, s));
+    uint32_t st = 0;
+    CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::memset(&c->last, 0, sizeof(c->last));
+    c->last.samples = (uint64_t)npix * P.spp;
+    c->last.render_launches = chunks;
+    c->last.kernel_launches = launches + 1;
+    if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
+    if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
+    if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
+}
+
 /* wavefront: trace all queued rays, shade all active paths, repeat until
  * every sample of the chunk has finished (rt_wavefront.cu) */
 void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
@@ -879,6 +940,10 @@ int rt_render(void* ctx, const rt_render_params* params, float* out_rgb) {
 int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render(c, params, d_out_rgb, false, (cudaStream_t)stream); });
+}
+int rt_render_device_noalloc(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render_noalloc(c, params, d_out_rgb, (cudaStream_t)stream); });
 }
 int rt_get_stats(void* ctx, rt_stats* out) {
     Ctx* c = (Ctx*)ctx;

@@ -15,6 +15,10 @@ cudaError_t rt_launch_accumulate(float* film, const float* samples, int64_t npix
 cudaError_t rt_launch_finalize(float* out, const float* film, int64_t npix, float spp, cudaStream_t stream);
 cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ,
                             uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
+/* device address of the fixed RT_NOALLOC_SCRATCH_BYTES scratch array on
+ * `device`, which must be the current device; looked up once per device and
+ * process (rt_noalloc.cu) */
+cudaError_t rt_noalloc_scratch(int device, void** ptr);
 cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream);
 
 #endif

@@ -101,6 +101,13 @@ class Device:
         p = settings.to_c()
         self._check(self.lib.rt_render_device(self.h, C.byref(p), C.c_void_p(out_ptr), C.c_void_p(stream or None)))
 
+    def render_device_noalloc(self, settings: RenderSettings, out_ptr: int, stream: int = 0):
+        """Same film as render_device, rendered out of the library's fixed device
+        scratch (RT_NOALLOC_SCRATCH_BYTES) with no device allocation."""
+        p = settings.to_c()
+        self._check(self.lib.rt_render_device_noalloc(self.h, C.byref(p), C.c_void_p(out_ptr),
+                                                      C.c_void_p(stream or None)))
+
     def trace_closest_device(self, rays_ptr: int, n: int, hits_ptr: int, stream: int = 0):
         self._check(self.lib.rt_trace_closest_device(self.h, C.c_void_p(rays_ptr), n, C.c_void_p(hits_ptr),
                                                      C.c_void_p(stream or None)))

@@ -134,9 +134,11 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_get_stats", "rt_set_counting", "rt_set_renderer", "rt_cancel",
+    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_get_stats", "rt_set_counting",
+    "rt_set_renderer", "rt_cancel",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT = 0, 1, 2
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024   # RT_NOALLOC_SCRATCH_BYTES
 
 _lib = None
 
@@ -165,6 +167,8 @@ def _declare(lib):
     lib.rt_render.argtypes = [vp, C.POINTER(RenderParams), vp]
     lib.rt_render_device.restype = C.c_int
     lib.rt_render_device.argtypes = [vp, C.POINTER(RenderParams), vp, vp]
+    lib.rt_render_device_noalloc.restype = C.c_int
+    lib.rt_render_device_noalloc.argtypes = [vp, C.POINTER(RenderParams), vp, vp]
     lib.rt_get_stats.restype = C.c_int
     lib.rt_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.rt_set_counting.restype = C.c_int
