@@ -375,205 +375,302 @@ struct Best {
     V3 pw;           /* for instance candidates: world-space point */
 };
 
-DF bool InstanceClosest(const RtSceneView* S, int inst, const Ray& ray, Best* b, int2* stack, uint32_t* status, TravStats* st);
-DF bool InstanceAny(const RtSceneView* S, int inst, const Ray& ray, int2* stack, uint32_t* status, TravStats* st);
-/* kTop: the top-level tree, whose leaves may be instances; a prototype tree
- * (kTop = false) holds triangles and spheres only, which keeps the nesting
- * one level deep at compile time. */
+#define RT_TRAVERSAL_CAP (1u << 26)   /* loop steps of one two-level traversal */
+#define RT_NO_NODE ((int)0x80000000)
 
-/* One leaf primitive for the closest-hit traversal; updates ray.MaxT like
- * Bvh.Intersect (Accelerators/Bvh.cs:193-204).  Returns true on a candidate hit. */
-template <bool kTop>
-DF void LeafClosest(const RtSceneView* S, int slot, Ray& ray, Best* best, bool* any, int2* stack, uint32_t* status, TravStats* st) {
-    float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
-    float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
-    float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
-    uint32_t kr = __float_as_uint(s1.w);
-    uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
-    if (st) st->prims++;
-    float t; float u = 0, v = 0; uint32_t fl = 0; int sub = -1; V3 pw = v3s(0);
+/* Leaf primitive of either level against ray r: triangle or sphere (the
+ * instance case is handled by the callers).  Bvh.Intersect's leaf loop
+ * (Accelerators/Bvh.cs:193-204, 140-152). */
+DF bool PrimHit(const RtSceneView* S, uint32_t kind, uint32_t ref, float4 s0, float4 s1, float4 s2, const Ray& r,
+                float* t, float* u, float* v) {
     if (kind == RT_KIND_TRI) {
         SurfPt sp;
-        if (!TriTest(f4xyz(s0), f4xyz(s1), f4xyz(s2), ray, &sp)) return;
-        t = sp.t; u = sp.u; v = sp.v;
-    } else if (kind == RT_KIND_SPHERE) {
-        RtSphere sph = S->spheres[ref];
-        if (!SphereTest(v3(sph.center[0], sph.center[1], sph.center[2]), sph.radius, ray, &t)) return;
-    } else if (kTop) {
-        Best ib;
-        if (!InstanceClosest(S, (int)ref, ray, &ib, stack + RT_STACK_SIZE, status, st)) return;
-        t = ib.t; u = ib.u; v = ib.v; fl = ib.flags; sub = ib.slot; pw = ib.pw;
-    } else {
-        atomicOr(status, RT_STATUS_BADREF);
-        return;
+        if (!TriTest(f4xyz(s0), f4xyz(s1), f4xyz(s2), r, &sp)) return false;
+        *t = sp.t; *u = sp.u; *v = sp.v;
+        return true;
     }
-    *any = true;
-    best->flags |= fl;
-    if (t < best->t) {
-        best->t = t; best->u = u; best->v = v; best->slot = slot; best->sub = sub; best->pw = pw;
-        ray.MaxT = t;
-    } else if (t == best->t) {
-        best->flags |= RT_HIT_TIE;
-    }
+    RtSphere sph = S->spheres[ref];
+    *u = 0; *v = 0;
+    return SphereTest(v3(sph.center[0], sph.center[1], sph.center[2]), sph.radius, r, t);
 }
 
-/* Bvh.Intersect(ray, out inct) (Accelerators/Bvh.cs:174-232): the same set of
- * boxes is tested in the same order against the same MaxT.  Both child boxes
- * are read from the parent; the far child is pushed with its entry distance
- * (or NaN when its slab test already failed) and re-checked against the MaxT
- * current when it is popped, exactly when the reference would test it. */
-template <bool kTop>
-DF bool BvhClosest(const RtSceneView* S, int bvh, Ray& ray, Best* best, int2* stack, uint32_t* status, TravStats* st) {
+/* Root box of tree `bvh`: RT_NO_NODE if the tree is empty or the box is
+ * missed, else the root's reference (counts one node visit if non-empty). */
+DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
     const RtBvh h = S->bvhs[bvh];
-    best->t = kFMax; best->flags = 0; best->slot = -1; best->sub = -1; best->u = 0; best->v = 0;
-    if (h.root_ref == (int)0x80000000) return false;
-    bool any = false;
+    if (h.root_ref == RT_NO_NODE) return RT_NO_NODE;
     if (st) st->nodes++;
     float tmin;
-    if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], ray, &tmin) || !(tmin < ray.MaxT))
-        return false;
-    const bool neg[3] = {ray.InvD.x < 0, ray.InvD.y < 0, ray.InvD.z < 0};
-    int sp = 0;
-    int cur = h.root_ref;
-    uint32_t guard = 0;
-    while (true) {
-        if (cur < 0) {
-            /* leaf */
-            int first = ~cur;
-            int count = __float_as_int(__ldg(S->slots + 3 * (int64_t)first + 2).w);
-            for (int i = 0; i < count; i++) LeafClosest<kTop>(S, first + i, ray, best, &any, stack, status, st);
-        } else {
-            if (++guard > (1u << 24)) { atomicOr(status, RT_STATUS_ITER); break; }
-            const float4* np = S->nodes + 4 * (int64_t)cur;
-            float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-            int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
-            float tl, tr;
-            bool al = SlabA(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ray, &tl);
-            bool ar = SlabA(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ray, &tr);
-            bool rightFirst = neg[axis];
-            int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
-            bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
-            float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
-            if (sp == RT_STACK_SIZE) { atomicOr(status, RT_STATUS_STACK); break; }
-            stack[sp++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
-            if (st) st->nodes++;
-            if (nearA && nearT < ray.MaxT) { cur = nearRef; continue; }
-        }
-        /* pop: the reference pops and tests the next box */
-        bool found = false;
-        while (sp > 0) {
-            int2 e = stack[--sp];
-            if (st) st->nodes++;
-            if (__int_as_float(e.y) < ray.MaxT) { cur = e.x; found = true; break; }
-        }
-        if (!found) break;
-    }
-    return any;
+    if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], r, &tmin) ||
+        !(tmin < r.MaxT))
+        return RT_NO_NODE;
+    return h.root_ref;
 }
 
-/* Bvh.Intersect(ray) any-hit (Accelerators/Bvh.cs:126-172) */
-template <bool kTop>
-DF bool BvhAny(const RtSceneView* S, int bvh, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
-    const RtBvh h = S->bvhs[bvh];
-    if (h.root_ref == (int)0x80000000) return false;
-    if (st) st->nodes++;
-    float tmin;
-    if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], ray, &tmin) || !(tmin < ray.MaxT))
-        return false;
-    const bool neg[3] = {ray.InvD.x < 0, ray.InvD.y < 0, ray.InvD.z < 0};
-    int sp = 0;
-    int cur = h.root_ref;
-    uint32_t guard = 0;
-    while (true) {
-        if (cur < 0) {
-            int first = ~cur;
-            int count = __float_as_int(__ldg(S->slots + 3 * (int64_t)first + 2).w);
-            for (int i = 0; i < count; i++) {
-                int slot = first + i;
-                float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
-                float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
-                float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
-                uint32_t kr = __float_as_uint(s1.w);
-                uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
-                if (st) st->prims++;
-                bool hit;
-                if (kind == RT_KIND_TRI) { SurfPt p; hit = TriTest(f4xyz(s0), f4xyz(s1), f4xyz(s2), ray, &p); }
-                else if (kind == RT_KIND_SPHERE) {
-                    RtSphere sph = S->spheres[ref]; float t;
-                    hit = SphereTest(v3(sph.center[0], sph.center[1], sph.center[2]), sph.radius, ray, &t);
-                } else if (kTop) {
-                    hit = InstanceAny(S, (int)ref, ray, stack + RT_STACK_SIZE, status, st);
-                } else {
-                    atomicOr(status, RT_STATUS_BADREF);
-                    hit = false;
+/* One interior node: both child boxes are read from the parent, the far child
+ * is pushed with its entry distance (NaN when its slab test already failed)
+ * and re-checked against the MaxT current when it is popped, which is exactly
+ * when the reference tests it.  Returns the near child to descend into, or
+ * RT_NO_NODE. */
+DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int* sp) {
+    const float4* np = S->nodes + 4 * (int64_t)node;
+    const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
+    const int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
+    float tl, tr;
+    const bool al = SlabA(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, r, &tl);
+    const bool ar = SlabA(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, r, &tr);
+    const float ia = axis == 0 ? r.InvD.x : (axis == 1 ? r.InvD.y : r.InvD.z);
+    const bool rightFirst = ia < 0;
+    const int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
+    const bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
+    const float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
+    stack[(*sp)++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
+    return (nearA && nearT < r.MaxT) ? nearRef : RT_NO_NODE;
+}
+
+/* Scene.Intersect(ray, out inct) over the two-level scene: Bvh.Intersect
+ * (Accelerators/Bvh.cs:174-232) on the top-level tree and, for each instance
+ * leaf, InstancedPrimitive.Intersect (Primitive.cs:169-188) on its prototype
+ * tree in model space with world T = Distance(ray.O, p).  Boxes, MaxT culls
+ * and primitive tests happen in exactly the order of the recursive form; the
+ * recursion is unrolled into a state machine whose every step is one leaf
+ * primitive, one node, one pop, or leaving a prototype.  Rays at different
+ * levels therefore run the same step code together, and a persistent kernel
+ * can hand a lane a new ray between any two steps.  stack[0, base) holds
+ * top-level entries, stack[base, base + RT_STACK_SIZE) the prototype's, so
+ * `stack` has 2 * RT_STACK_SIZE entries. */
+struct TravClosest {
+    Ray r;                       /* world ray, or the model-space ray inside a prototype */
+    V3 wO, wD;                   /* the world ray */
+    float wMaxT;                 /* the world ray's MaxT while a prototype is traversed */
+    Best best;
+    float pt, pu, pv; int pslot; uint32_t pflags;     /* the prototype's own closest hit */
+    int cur, sp, base, leafSlot, leafLeft, topSlot, topLeft, inst;
+    bool any, inProto, pany;
+    uint32_t guard;
+};
+
+/* Returns true when the traversal is already over (empty scene or root box missed). */
+DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravStats* st) {
+    Best& b = T.best;
+    b.t = kFMax; b.flags = 0; b.slot = -1; b.sub = -1; b.u = 0; b.v = 0; b.pw = v3s(0);
+    T.r = ray; T.wO = ray.O; T.wD = ray.D; T.wMaxT = ray.MaxT;
+    T.any = false; T.inProto = false; T.pany = false;
+    T.base = 0; T.sp = 0; T.leafLeft = 0; T.leafSlot = 0; T.topSlot = 0; T.topLeft = 0; T.inst = 0;
+    T.pt = kFMax; T.pu = 0; T.pv = 0; T.pslot = -1; T.pflags = 0;
+    T.guard = 0;
+    T.cur = RootRef(S, 0, ray, st);
+    return T.cur == RT_NO_NODE;
+}
+
+/* One step; true when the traversal has finished. */
+DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t* status, TravStats* st) {
+    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (T.leafLeft > 0) {
+        const int slot = T.leafSlot++;
+        T.leafLeft--;
+        const float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
+        const float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
+        const float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
+        const uint32_t kr = __float_as_uint(s1.w);
+        const uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
+        if (st) st->prims++;
+        if (kind != RT_KIND_INSTANCE) {
+            float t, u, v;
+            if (!PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) return false;
+            if (T.inProto) {
+                T.pany = true;
+                if (t < T.pt) { T.pt = t; T.pu = u; T.pv = v; T.pslot = slot; T.r.MaxT = t; }
+                else if (t == T.pt) T.pflags |= RT_HIT_TIE;
+            } else {
+                T.any = true;
+                if (t < T.best.t) {
+                    T.best.t = t; T.best.u = u; T.best.v = v; T.best.slot = slot; T.best.sub = -1; T.best.pw = v3s(0);
+                    T.r.MaxT = t;
+                } else if (t == T.best.t) {
+                    T.best.flags |= RT_HIT_TIE;
                 }
-                if (hit) return true;
             }
-        } else {
-            if (++guard > (1u << 24)) { atomicOr(status, RT_STATUS_ITER); return false; }
-            const float4* np = S->nodes + 4 * (int64_t)cur;
-            float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
-            int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
-            float tl, tr;
-            bool al = SlabA(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, ray, &tl);
-            bool ar = SlabA(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, ray, &tr);
-            bool rightFirst = neg[axis];
-            int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
-            bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
-            float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
-            if (sp == RT_STACK_SIZE) { atomicOr(status, RT_STATUS_STACK); return false; }
-            stack[sp++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
-            if (st) st->nodes++;
-            if (nearA && nearT < ray.MaxT) { cur = nearRef; continue; }
+            return false;
         }
-        bool found = false;
-        while (sp > 0) {
-            int2 e = stack[--sp];
-            if (st) st->nodes++;
-            if (__int_as_float(e.y) < ray.MaxT) { cur = e.x; found = true; break; }
-        }
-        if (!found) break;
+        if (T.inProto) { atomicOr(status, RT_STATUS_BADREF); return false; }
+        /* enter the instance's prototype */
+        if (st) st->insts++;
+        T.inst = (int)ref;
+        T.topSlot = T.leafSlot; T.topLeft = T.leafLeft; T.leafLeft = 0;
+        T.wMaxT = T.r.MaxT;
+        const RtInstance& I = S->instances[T.inst];
+        float w2m[12];
+#pragma unroll
+        for (int i = 0; i < 12; i++) w2m[i] = __ldg(I.w2m + i);
+        T.r = XfRay(T.r, w2m);
+        T.pt = kFMax; T.pu = 0; T.pv = 0; T.pslot = -1; T.pflags = 0; T.pany = false;
+        T.inProto = true;
+        T.base = T.sp;
+        T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        return false;
     }
+    if (T.cur != RT_NO_NODE) {
+        if (T.cur < 0) {
+            T.leafSlot = ~T.cur;
+            T.leafLeft = __float_as_int(__ldg(S->slots + 3 * (int64_t)T.leafSlot + 2).w);
+            T.cur = RT_NO_NODE;
+            return false;
+        }
+        if (T.sp - T.base == RT_STACK_SIZE) {
+            atomicOr(status, RT_STATUS_STACK);
+            if (!T.inProto) return true;
+            T.sp = T.base;                      /* the prototype's traversal stops here */
+            T.cur = RT_NO_NODE;
+            return false;
+        }
+        if (st) st->nodes++;
+        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp);
+        return false;
+    }
+    if (T.sp > T.base) {
+        const int2 e = stack[--T.sp];
+        if (st) st->nodes++;
+        if (__int_as_float(e.y) < T.r.MaxT) T.cur = e.x;
+        return false;
+    }
+    if (!T.inProto) return true;
+    /* leave the prototype: the instance's candidate in world space */
+    T.inProto = false;
+    if (T.pany) {
+        const RtInstance& I = S->instances[T.inst];
+        const float4 s1 = __ldg(S->slots + 3 * (int64_t)T.pslot + 1);
+        const uint32_t kr = __float_as_uint(s1.w);
+        V3 pm;
+        if ((kr >> RT_KIND_SHIFT) == RT_KIND_TRI) {
+            const V3 bary = v3(1 - (T.pu + T.pv), T.pu, T.pv);
+            const RtTri t = S->tris[kr & RT_REF_MASK];
+            pm = bary.x * f4xyz(S->pos[t.v0]) + bary.y * f4xyz(S->pos[t.v1]) + bary.z * f4xyz(S->pos[t.v2]);
+        } else {
+            const RtSphere sph = S->spheres[kr & RT_REF_MASK];
+            const V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
+            const V3 n = Normalize(At(T.r, T.pt) - c);
+            pm = n * sph.radius + c;
+        }
+        float m2w[12];
+#pragma unroll
+        for (int i = 0; i < 12; i++) m2w[i] = __ldg(I.m2w + i);
+        const V3 pw = Xf12(pm, m2w);
+        const float t = Distance(T.wO, pw);
+        T.any = true;
+        T.best.flags |= T.pflags;
+        if (t < T.best.t) {
+            T.best.t = t; T.best.u = T.pu; T.best.v = T.pv; T.best.slot = T.topSlot - 1; T.best.sub = T.pslot; T.best.pw = pw;
+            T.wMaxT = t;
+        } else if (t == T.best.t) {
+            T.best.flags |= RT_HIT_TIE;
+        }
+    }
+    T.r = mkray(T.wO, T.wD, T.r.MinT, T.wMaxT);
+    T.leafSlot = T.topSlot; T.leafLeft = T.topLeft;
+    T.sp = T.base;
+    T.base = 0;
     return false;
 }
 
-/* InstancedPrimitive.Intersect (Primitive.cs:169-188): prototype traversal in
- * model space, world T = Distance(ray.O, p). */
-DF bool InstanceClosest(const RtSceneView* S, int inst, const Ray& ray, Best* b, int2* stack, uint32_t* status, TravStats* st) {
-    if (st) st->insts++;
-    const RtInstance& I = S->instances[inst];
-    float w2m[12], m2w[12];
-#pragma unroll
-    for (int i = 0; i < 12; i++) { w2m[i] = __ldg(I.w2m + i); m2w[i] = __ldg(I.m2w + i); }
-    Ray mr = XfRay(ray, w2m);
-    Best mb;
-    if (!BvhClosest<false>(S, 1 + __ldg(&I.blas), mr, &mb, stack, status, st)) return false;
-    /* model-space point of the winning prototype primitive */
-    float4 s1 = __ldg(S->slots + 3 * (int64_t)mb.slot + 1);
-    uint32_t kr = __float_as_uint(s1.w);
-    V3 pm;
-    if ((kr >> RT_KIND_SHIFT) == RT_KIND_TRI) {
-        V3 bary = v3(1 - (mb.u + mb.v), mb.u, mb.v);
-        RtTri t = S->tris[kr & RT_REF_MASK];
-        pm = bary.x * f4xyz(S->pos[t.v0]) + bary.y * f4xyz(S->pos[t.v1]) + bary.z * f4xyz(S->pos[t.v2]);
-    } else {
-        RtSphere sph = S->spheres[kr & RT_REF_MASK];
-        V3 c = v3(sph.center[0], sph.center[1], sph.center[2]);
-        V3 n = Normalize(At(mr, mb.t) - c);
-        pm = n * sph.radius + c;
-    }
-    V3 pw = Xf12(pm, m2w);
-    b->t = Distance(ray.O, pw); b->u = mb.u; b->v = mb.v; b->slot = mb.slot; b->flags = mb.flags; b->pw = pw; b->sub = -1;
-    return true;
+/* The whole closest-hit traversal of one ray; ray.MaxT ends at the closest hit. */
+DF bool SceneClosest(const RtSceneView* S, Ray& ray, Best* best, int2* stack, uint32_t* status, TravStats* st) {
+    TravClosest T;
+    if (!ClosestBegin(S, ray, T, st))
+        while (!ClosestStep(S, T, stack, status, st)) {}
+    *best = T.best;
+    ray.MaxT = T.inProto ? T.wMaxT : T.r.MaxT;
+    return T.any;
 }
-DF bool InstanceAny(const RtSceneView* S, int inst, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
-    if (st) st->insts++;
-    const RtInstance& I = S->instances[inst];
-    float w2m[12];
+
+/* Scene.Intersect(ray): the any-hit form (Bvh.cs:126-172,
+ * InstancedPrimitive.Intersect(ray), Primitive.cs:162-167). */
+struct TravAny {
+    Ray r;
+    V3 wO, wD;
+    float wMaxT;
+    int cur, sp, base, leafSlot, leafLeft, topSlot, topLeft;
+    bool inProto, hit;
+    uint32_t guard;
+};
+
+DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st) {
+    T.r = ray; T.wO = ray.O; T.wD = ray.D; T.wMaxT = ray.MaxT;
+    T.inProto = false; T.hit = false;
+    T.base = 0; T.sp = 0; T.leafLeft = 0; T.leafSlot = 0; T.topSlot = 0; T.topLeft = 0;
+    T.guard = 0;
+    T.cur = RootRef(S, 0, ray, st);
+    return T.cur == RT_NO_NODE;
+}
+
+/* One step; true when the traversal has finished (T.hit holds the answer). */
+DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status, TravStats* st) {
+    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (T.leafLeft > 0) {
+        const int slot = T.leafSlot++;
+        T.leafLeft--;
+        const float4 s0 = __ldg(S->slots + 3 * (int64_t)slot);
+        const float4 s1 = __ldg(S->slots + 3 * (int64_t)slot + 1);
+        const float4 s2 = __ldg(S->slots + 3 * (int64_t)slot + 2);
+        const uint32_t kr = __float_as_uint(s1.w);
+        const uint32_t kind = kr >> RT_KIND_SHIFT, ref = kr & RT_REF_MASK;
+        if (st) st->prims++;
+        if (kind != RT_KIND_INSTANCE) {
+            float t, u, v;
+            if (PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) { T.hit = true; return true; }
+            return false;
+        }
+        if (T.inProto) { atomicOr(status, RT_STATUS_BADREF); return false; }
+        if (st) st->insts++;
+        T.topSlot = T.leafSlot; T.topLeft = T.leafLeft; T.leafLeft = 0;
+        const RtInstance& I = S->instances[(int)ref];
+        float w2m[12];
 #pragma unroll
-    for (int i = 0; i < 12; i++) w2m[i] = __ldg(I.w2m + i);
-    Ray mr = XfRay(ray, w2m);
-    return BvhAny<false>(S, 1 + __ldg(&I.blas), mr, stack, status, st);
+        for (int i = 0; i < 12; i++) w2m[i] = __ldg(I.w2m + i);
+        T.r = XfRay(T.r, w2m);
+        T.inProto = true;
+        T.base = T.sp;
+        T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        return false;
+    }
+    if (T.cur != RT_NO_NODE) {
+        if (T.cur < 0) {
+            T.leafSlot = ~T.cur;
+            T.leafLeft = __float_as_int(__ldg(S->slots + 3 * (int64_t)T.leafSlot + 2).w);
+            T.cur = RT_NO_NODE;
+            return false;
+        }
+        if (T.sp - T.base == RT_STACK_SIZE) {
+            atomicOr(status, RT_STATUS_STACK);
+            if (!T.inProto) return true;
+            T.sp = T.base;
+            T.cur = RT_NO_NODE;
+            return false;
+        }
+        if (st) st->nodes++;
+        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp);
+        return false;
+    }
+    if (T.sp > T.base) {
+        const int2 e = stack[--T.sp];
+        if (st) st->nodes++;
+        if (__int_as_float(e.y) < T.r.MaxT) T.cur = e.x;
+        return false;
+    }
+    if (!T.inProto) return true;
+    T.inProto = false;
+    T.r = mkray(T.wO, T.wD, T.r.MinT, T.wMaxT);
+    T.leafSlot = T.topSlot; T.leafLeft = T.topLeft;
+    T.sp = T.base;
+    T.base = 0;
+    return false;
+}
+
+DF bool SceneAny(const RtSceneView* S, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
+    TravAny T;
+    if (!AnyBegin(S, ray, T, st))
+        while (!AnyStep(S, T, stack, status, st)) {}
+    return T.hit;
 }
 
 /* Builds the full Intersection of the winning primitive (GetIntersection /

@@ -78,7 +78,7 @@ struct Ctx {
     WfState wf{};
     std::vector<DevBuf> wf_bufs;
     int wf_slots = 0;
-    int32_t* wf_counters = nullptr;            /* [0] rays queued, [1] / [2] active lists */
+    int32_t* wf_counters = nullptr;            /* [0] rays queued, [1] / [2] active lists, [3] shadow rays, [4] / [5] fetch */
     int32_t* h_counts = nullptr;               /* pinned mirror of wf_counters */
     int wf_capacity = 1 << 21;                 /* path slots in flight */
 };
@@ -145,6 +145,8 @@ void ensure_wf(Ctx* c, int slots) {
     const size_t n = (size_t)slots, q = 3 * (size_t)slots;
     W.q_o = wf_alloc<float4>(c, q); W.q_d = wf_alloc<float4>(c, q); W.q_meta = wf_alloc<int32_t>(c, q);
     W.active = wf_alloc<int32_t>(c, n); W.active_next = wf_alloc<int32_t>(c, n);
+    W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint8_t>(c, n);
+    W.key_count = wf_alloc<int32_t>(c, 32);
     W.next_sample = wf_alloc<unsigned long long>(c, 1);
     W.pix = wf_alloc<int4>(c, n); W.rng_n = wf_alloc<uint32_t>(c, n);
     W.coeff = wf_alloc<float4>(c, n); W.rad = wf_alloc<float4>(c, n);
@@ -156,7 +158,7 @@ void ensure_wf(Ctx* c, int slots) {
     W.ext_hit = wf_alloc<float4>(c, n); W.ext_sub = wf_alloc<int32_t>(c, n);
     W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
     W.occluded = wf_alloc<uint8_t>(c, n);
-    if (!c->wf_counters) CK(cudaMalloc((void**)&c->wf_counters, 4 * sizeof(int32_t)));
+    if (!c->wf_counters) CK(cudaMalloc((void**)&c->wf_counters, 8 * sizeof(int32_t)));
     if (!c->h_counts) CK(cudaMallocHost((void**)&c->h_counts, 4 * sizeof(int32_t)));
     c->wf_slots = slots;
 }
@@ -765,6 +767,7 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     W.n_rays_next = c->wf_counters;
     W.n_shadow_next = c->wf_counters + 3;
     W.shadow_base = 2 * slots;
+    W.fetch = c->wf_counters + 4;
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
     for (int b = 0; b < P.spp; b += chunk) {
@@ -791,9 +794,9 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
             CK(cudaMemsetAsync(W.n_shadow_next, 0, sizeof(int32_t), s));
             CK(cudaMemsetAsync(W.n_active_next, 0, sizeof(int32_t), s));
             CK(cudaEventRecord(c->events[2], s));
-            CK(rt_wf_shade(c->d_view, P, W, n_active, c->status, c->stats, c->counting, true, s));
+            CK(rt_wf_shade(c->d_view, P, W, n_active, c->status, c->stats, c->counting, true, s, &launches));
             CK(cudaEventRecord(c->events[3], s));
-            launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0) + 1;
+            launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0);
             trace_launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0);
             std::swap(W.active, W.active_next);
             std::swap(W.n_active, W.n_active_next);

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(const RtSceneView* __rest
     Ray r = ray;
     Best b;
     rt_hit h;
-    if (BvhClosest<true>(S, 0, r, &b, stack, status, counting ? &st : nullptr)) {
+    if (SceneClosest(S, r, &b, stack, status, counting ? &st : nullptr)) {
         Isect it;
         Finish(S, ray, b, &it);
         h.t = it.T; h.u = it.bu; h.v = it.bv; h.prim = it.prim; h.sub = it.sub; h.flags = it.flags;
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(128) k_trace_any(const RtSceneView* __restrict
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
     Ray ray = ray_from(rays[i]);
-    occ[i] = BvhAny<true>(S, 0, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
+    occ[i] = SceneAny(S, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
     if (counting) {
         warp_add(stats + 3, st.nodes);
         warp_add(stats + 4, st.prims);

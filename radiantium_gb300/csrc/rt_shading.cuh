@@ -29,13 +29,13 @@ NF bool SceneIntersect(Ctx& c, const Ray& ray, Isect* it) {
     if (c.st) c.rays_closest++;
     Ray r = ray;
     Best b;
-    if (!BvhClosest<true>(c.S, 0, r, &b, c.stack, c.status, c.st)) return false;
+    if (!SceneClosest(c.S, r, &b, c.stack, c.status, c.st)) return false;
     Finish(c.S, ray, b, it);
     return true;
 }
 NF bool SceneIntersectP(Ctx& c, const Ray& ray) {
     if (c.st) c.rays_shadow++;
-    return BvhAny<true>(c.S, 0, ray, c.stack, c.status, c.st);
+    return SceneAny(c.S, ray, c.stack, c.status, c.st);
 }
 DF const RtPrim& PrimOf(const RtSceneView* S, const Isect& it) { return S->prims[it.prim]; }
 DF bool HasSurface(const RtSceneView* S, const Isect& it) { return S->prims[it.prim].material >= 0; }

@@ -7,7 +7,10 @@
  *
  *   k_wf_trace_closest / k_wf_trace_shadow   the queued rays: extension and
  *                MIS rays (closest hit), shadow rays (any hit), each kind in
- *                its own kernel so the two traversal loops never share a warp;
+ *                its own persistent kernel with dynamic ray fetch;
+ *   k_wf_sort_count / k_wf_sort_scatter   regroup the active list by shade
+ *                key (finished, missed, material type) so that a warp runs
+ *                one material's code instead of the union of several;
  *   k_wf_shade   per path: first adds the direct-lighting term scheduled in
  *                the previous shade (its shadow / MIS rays are now resolved),
  *                then runs one bounce of the reference loop on the new
@@ -21,6 +24,7 @@
  * camera sample, which keeps the queues full to the end of a render.
  */
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "rt_integrators.cuh"
 #include "rt_wavefront.h"
 
@@ -126,24 +130,64 @@ __global__ void __launch_bounds__(256) k_wf_start(const RtSceneView* __restrict_
     start_path(S, P, W, slot, true);
 }
 
+/* Persistent traversal with dynamic ray fetch (Aila & Laine 2009): each warp
+ * keeps its lanes busy by handing a new queue entry to every lane whose ray
+ * has finished, as soon as kRefill lanes are idle, instead of idling until
+ * the warp's longest ray is done.  The traversal is the step machine of
+ * TravClosest / TravAny, so a lane can take a new ray between any two steps
+ * and the per-ray results are the same as a one-ray-per-thread launch. */
+constexpr unsigned kFullWarp = 0xffffffffu;
+constexpr int kRefill = 8;
+
+/* One warp-wide fetch: returns this lane's queue entry (>= n: none) and sets
+ * `exhausted` (warp-uniform) once the queue has been handed out. */
+DF int fetch_entry(int32_t* counter, int n, unsigned idle, bool* exhausted) {
+    const unsigned lane = threadIdx.x & 31;
+    int first = 0;
+    if (lane == 0) first = atomicAdd(counter, __popc(idle));
+    first = __shfl_sync(kFullWarp, first, 0);
+    *exhausted = first + __popc(idle) >= n;
+    return first + __popc(idle & ((1u << lane) - 1u));
+}
+
+DF Ray queued_ray(const WfState& W, int q) {
+    const float4 o = W.q_o[q], d = W.q_d[q];
+    return mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
+}
+
+DF void closest_done(const WfState& W, int q, const TravClosest& T) {
+    const int meta = W.q_meta[q];
+    const int path = meta >> 2;
+    const float4 h = make_float4(T.best.t, T.best.u, T.best.v, __int_as_float(T.any ? T.best.slot : -1));
+    if ((meta & 3) == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = T.best.sub; }
+    else { W.mis_hit[path] = h; W.mis_sub[path] = T.best.sub; }
+}
+
 /* closest-hit rays: extension and MIS rays (queue [0, n)) */
 __global__ void __launch_bounds__(128) k_wf_trace_closest(const RtSceneView* __restrict__ S, WfState W, int n,
                                                             uint32_t* status, unsigned long long* stats, bool counting) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 o = W.q_o[i], d = W.q_d[i];
-    const int meta = W.q_meta[i];
-    const int path = meta >> 2, kind = meta & 3;
-    Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
-    Best b;
-    bool hit = BvhClosest<true>(S, 0, ray, &b, stack, status, counting ? &st : nullptr);
-    float4 h = make_float4(b.t, b.u, b.v, __int_as_float(hit ? b.slot : -1));
-    if (kind == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = b.sub; }
-    else { W.mis_hit[path] = h; W.mis_sub[path] = b.sub; }
+    TravStats* pst = counting ? &st : nullptr;
+    uint32_t done = 0;
+    TravClosest T;
+    int item = -1;
+    bool exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(kFullWarp, item < 0);
+        if (exhausted) {
+            if (idle == kFullWarp) break;
+        } else if (__popc(idle) >= kRefill) {
+            const int q = fetch_entry(W.fetch, n, idle, &exhausted);
+            if (item < 0 && q < n) {
+                if (ClosestBegin(S, queued_ray(W, q), T, pst)) { closest_done(W, q, T); done++; }
+                else item = q;
+            }
+        }
+        if (item >= 0 && ClosestStep(S, T, stack, status, pst)) { closest_done(W, item, T); done++; item = -1; }
+    }
     if (counting) {
-        warp_add64(stats + 1, 1u);
+        warp_add64(stats + 1, done);
         warp_add64(stats + 3, st.nodes);
         warp_add64(stats + 4, st.prims);
         warp_add64(stats + 5, st.insts);
@@ -153,17 +197,33 @@ __global__ void __launch_bounds__(128) k_wf_trace_closest(const RtSceneView* __r
 /* shadow rays: any-hit (queue [shadow_base, shadow_base + n)) */
 __global__ void __launch_bounds__(128) k_wf_trace_shadow(const RtSceneView* __restrict__ S, WfState W, int n,
                                                            uint32_t* status, unsigned long long* stats, bool counting) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int q = W.shadow_base + i;
-    const float4 o = W.q_o[q], d = W.q_d[q];
-    const int path = W.q_meta[q] >> 2;
-    Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
-    W.occluded[path] = BvhAny<true>(S, 0, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
+    TravStats* pst = counting ? &st : nullptr;
+    uint32_t done = 0;
+    TravAny T;
+    int item = -1;
+    bool exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(kFullWarp, item < 0);
+        if (exhausted) {
+            if (idle == kFullWarp) break;
+        } else if (__popc(idle) >= kRefill) {
+            const int e = fetch_entry(W.fetch + 1, n, idle, &exhausted);
+            if (item < 0 && e < n) {
+                const int q = W.shadow_base + e;
+                if (AnyBegin(S, queued_ray(W, q), T, pst)) { W.occluded[W.q_meta[q] >> 2] = 0; done++; }
+                else item = q;
+            }
+        }
+        if (item >= 0 && AnyStep(S, T, stack, status, pst)) {
+            W.occluded[W.q_meta[item] >> 2] = T.hit ? 1 : 0;
+            done++;
+            item = -1;
+        }
+    }
     if (counting) {
-        warp_add64(stats + 2, 1u);
+        warp_add64(stats + 2, done);
         warp_add64(stats + 3, st.nodes);
         warp_add64(stats + 4, st.prims);
         warp_add64(stats + 5, st.insts);
@@ -446,18 +506,88 @@ cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& 
     return cudaGetLastError();
 }
 
+/* resident blocks of a persistent trace kernel: every SM filled once */
+template <typename K>
+int persistent_blocks(K kernel, int n) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess || per_sm <= 0)
+        per_sm = 1, sms = sms > 0 ? sms : 1;
+    const int64_t need = ((int64_t)n + 127) / 128;
+    return (int)std::min<int64_t>(need, (int64_t)sms * per_sm);
+}
+
 cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
                         unsigned long long* stats, bool counting, cudaStream_t s) {
-    if (n_closest > 0) k_wf_trace_closest<<<grid_for(n_closest, 128), 128, 0, s>>>(S, W, n_closest, status, stats, counting);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(W.fetch, 0, 2 * sizeof(int32_t), s);
     if (e != cudaSuccess) return e;
-    if (n_shadow > 0) k_wf_trace_shadow<<<grid_for(n_shadow, 128), 128, 0, s>>>(S, W, n_shadow, status, stats, counting);
+    if (n_closest > 0)
+        k_wf_trace_closest<<<persistent_blocks(k_wf_trace_closest, n_closest), 128, 0, s>>>(S, W, n_closest, status, stats, counting);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (n_shadow > 0)
+        k_wf_trace_shadow<<<persistent_blocks(k_wf_trace_shadow, n_shadow), 128, 0, s>>>(S, W, n_shadow, status, stats, counting);
     return cudaGetLastError();
 }
 
+/* Shade key of an active path: which code the shade kernel will run for it.
+ * 0 finished (pending term, then a new sample), 1 missed the scene, 2 hit a
+ * medium boundary without a surface, 3 + RT_MAT_* hit that material type. */
+constexpr int kShadeKeys = 16;
+DF int shade_key(const RtSceneView* S, const WfState& W, int slot) {
+    if (W.flags[slot] & F_DONE) return 0;
+    const int hs = __float_as_int(W.ext_hit[slot].w);
+    if (hs < 0) return 1;
+    const int prim = __float_as_int(__ldg(S->slots + 3 * (int64_t)hs).w);
+    const int m = S->prims[prim].material;
+    if (m < 0) return 2;
+    return min(3 + S->materials[m].type, kShadeKeys - 1);
+}
+
+__global__ void __launch_bounds__(256) k_wf_sort_count(const RtSceneView* __restrict__ S, WfState W, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int key = shade_key(S, W, W.active[i]);
+    W.sort_key[i] = (uint8_t)key;
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.key_count + key, __popc(peers));
+}
+
+/* counting-sort scatter: entries of one key stay together, in any order
+ * (every path's result is independent of the order paths are shaded in) */
+__global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W, int n) {
+    __shared__ int base[kShadeKeys];
+    if (threadIdx.x < kShadeKeys) {
+        int b = 0;
+        for (int k = 0; k < (int)threadIdx.x; k++) b += W.key_count[k];
+        base[threadIdx.x] = b;
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int key = W.sort_key[i];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if ((int)lane == leader) first = atomicAdd(W.key_count + kShadeKeys + key, __popc(peers));
+    first = __shfl_sync(peers, first, leader);
+    W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[i];
+}
+
 cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
-                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s) {
+                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s, uint64_t* launches) {
     if (n <= 0) return cudaSuccess;
-    k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(S, P, W, n, status, stats, counting, regenerate);
+    WfState Ws = W;
+    if (n >= 4096) {
+        cudaError_t e = cudaMemsetAsync(W.key_count, 0, 2 * kShadeKeys * sizeof(int32_t), s);
+        if (e != cudaSuccess) return e;
+        k_wf_sort_count<<<grid_for(n, 256), 256, 0, s>>>(S, W, n);
+        k_wf_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(W, n);
+        *launches += 2;
+        Ws.active = W.sorted;
+    }
+    k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(S, P, Ws, n, status, stats, counting, regenerate);
+    *launches += 1;
     return cudaGetLastError();
 }

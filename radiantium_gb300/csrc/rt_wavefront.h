@@ -19,8 +19,12 @@ struct WfState {
     int32_t* n_rays_next;
     int32_t* n_shadow_next;
     int32_t shadow_base;
+    int32_t* fetch;              /* [0] closest, [1] shadow: next queue entry to hand out */
     /* active slot lists (read by the shade kernel / written for the next one) */
     int32_t* active; int32_t* active_next;
+    /* the active list regrouped by shade key before shading (see shade_key) */
+    int32_t* sorted; uint8_t* sort_key;
+    int32_t* key_count;      /* [0, 16) entries per key, [16, 32) scatter cursors */
     int32_t* n_active; int32_t* n_active_next;
     unsigned long long* next_sample;
     /* path state */
@@ -47,7 +51,8 @@ struct WfState {
 cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& W, int slots, cudaStream_t s);
 cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
                         unsigned long long* stats, bool counting, cudaStream_t s);
+/* Shades the n active paths; launches += the kernels it started. */
 cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
-                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s);
+                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s, uint64_t* launches);
 
 #endif
