@@ -408,11 +408,15 @@ DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
 }
 
 /* One interior node: both child boxes are read from the parent, the far child
- * is pushed with its entry distance (NaN when its slab test already failed)
- * and re-checked against the MaxT current when it is popped, which is exactly
- * when the reference tests it.  Returns the near child to descend into, or
+ * is pushed with its entry distance and re-checked against the MaxT current
+ * when it is popped, which is exactly when the reference tests it.  A far
+ * child whose slab test already failed is pushed by the reference only to be
+ * rejected when popped (NaN < MaxT is false), so it is not stored at all -
+ * except while counting node visits (an any-hit traversal that stops early
+ * never pops, nor counts, what is left on its stack) and for trees tall
+ * enough to overflow the stack.  Returns the near child to descend into, or
  * RT_NO_NODE. */
-DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int* sp) {
+DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int* sp, TravStats* st) {
     const float4* np = S->nodes + 4 * (int64_t)node;
     const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
     const int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
@@ -424,8 +428,27 @@ DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int*
     const int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
     const bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
     const float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
-    stack[(*sp)++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
+    if (farA || st || S->deep_trees) stack[(*sp)++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
     return (nearA && nearT < r.MaxT) ? nearRef : RT_NO_NODE;
+}
+
+/* Pops until an entry passes the MaxT check (Bvh.cs:205-229 / 153-169). */
+DF int PopNext(int2* stack, int* sp, int base, float maxT, TravStats* st) {
+    while (*sp > base) {
+        const int2 e = stack[--*sp];
+        if (st) st->nodes++;
+        if (__int_as_float(e.y) < maxT) return e.x;
+    }
+    return RT_NO_NODE;
+}
+
+/* Leaf references become a primitive cursor (count in the first slot). */
+DF void EnterLeaf(const RtSceneView* S, int* cur, int* leafSlot, int* leafLeft) {
+    if (*cur != RT_NO_NODE && *cur < 0) {
+        *leafSlot = ~*cur;
+        *leafLeft = __float_as_int(__ldg(S->slots + 3 * (int64_t)*leafSlot + 2).w);
+        *cur = RT_NO_NODE;
+    }
 }
 
 /* Scene.Intersect(ray, out inct) over the two-level scene: Bvh.Intersect
@@ -460,7 +483,9 @@ DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravS
     T.pt = kFMax; T.pu = 0; T.pv = 0; T.pslot = -1; T.pflags = 0;
     T.guard = 0;
     T.cur = RootRef(S, 0, ray, st);
-    return T.cur == RT_NO_NODE;
+    if (T.cur == RT_NO_NODE) return true;
+    EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+    return false;
 }
 
 /* One step; true when the traversal has finished. */
@@ -477,8 +502,8 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
         if (st) st->prims++;
         if (kind != RT_KIND_INSTANCE) {
             float t, u, v;
-            if (!PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) return false;
-            if (T.inProto) {
+            if (!PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) {
+            } else if (T.inProto) {
                 T.pany = true;
                 if (t < T.pt) { T.pt = t; T.pu = u; T.pv = v; T.pslot = slot; T.r.MaxT = t; }
                 else if (t == T.pt) T.pflags |= RT_HIT_TIE;
@@ -491,9 +516,16 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
                     T.best.flags |= RT_HIT_TIE;
                 }
             }
+        } else if (T.inProto) {
+            atomicOr(status, RT_STATUS_BADREF);
+        }
+        if (kind != RT_KIND_INSTANCE || T.inProto) {
+            if (T.leafLeft == 0) {
+                T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+                EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+            }
             return false;
         }
-        if (T.inProto) { atomicOr(status, RT_STATUS_BADREF); return false; }
         /* enter the instance's prototype */
         if (st) st->insts++;
         T.inst = (int)ref;
@@ -508,15 +540,10 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
         T.inProto = true;
         T.base = T.sp;
         T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        if (T.cur < 0) {
-            T.leafSlot = ~T.cur;
-            T.leafLeft = __float_as_int(__ldg(S->slots + 3 * (int64_t)T.leafSlot + 2).w);
-            T.cur = RT_NO_NODE;
-            return false;
-        }
         if (T.sp - T.base == RT_STACK_SIZE) {
             atomicOr(status, RT_STATUS_STACK);
             if (!T.inProto) return true;
@@ -525,13 +552,9 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
             return false;
         }
         if (st) st->nodes++;
-        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp);
-        return false;
-    }
-    if (T.sp > T.base) {
-        const int2 e = stack[--T.sp];
-        if (st) st->nodes++;
-        if (__int_as_float(e.y) < T.r.MaxT) T.cur = e.x;
+        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+        if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
     if (!T.inProto) return true;
@@ -570,6 +593,10 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
     T.leafSlot = T.topSlot; T.leafLeft = T.topLeft;
     T.sp = T.base;
     T.base = 0;
+    if (T.leafLeft == 0) {
+        T.cur = PopNext(stack, &T.sp, 0, T.r.MaxT, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+    }
     return false;
 }
 
@@ -600,7 +627,9 @@ DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st
     T.base = 0; T.sp = 0; T.leafLeft = 0; T.leafSlot = 0; T.topSlot = 0; T.topLeft = 0;
     T.guard = 0;
     T.cur = RootRef(S, 0, ray, st);
-    return T.cur == RT_NO_NODE;
+    if (T.cur == RT_NO_NODE) return true;
+    EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+    return false;
 }
 
 /* One step; true when the traversal has finished (T.hit holds the answer). */
@@ -618,9 +647,16 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status,
         if (kind != RT_KIND_INSTANCE) {
             float t, u, v;
             if (PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) { T.hit = true; return true; }
+        } else if (T.inProto) {
+            atomicOr(status, RT_STATUS_BADREF);
+        }
+        if (kind != RT_KIND_INSTANCE || T.inProto) {
+            if (T.leafLeft == 0) {
+                T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+                EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+            }
             return false;
         }
-        if (T.inProto) { atomicOr(status, RT_STATUS_BADREF); return false; }
         if (st) st->insts++;
         T.topSlot = T.leafSlot; T.topLeft = T.leafLeft; T.leafLeft = 0;
         const RtInstance& I = S->instances[(int)ref];
@@ -631,15 +667,10 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status,
         T.inProto = true;
         T.base = T.sp;
         T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        if (T.cur < 0) {
-            T.leafSlot = ~T.cur;
-            T.leafLeft = __float_as_int(__ldg(S->slots + 3 * (int64_t)T.leafSlot + 2).w);
-            T.cur = RT_NO_NODE;
-            return false;
-        }
         if (T.sp - T.base == RT_STACK_SIZE) {
             atomicOr(status, RT_STATUS_STACK);
             if (!T.inProto) return true;
@@ -648,13 +679,9 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status,
             return false;
         }
         if (st) st->nodes++;
-        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp);
-        return false;
-    }
-    if (T.sp > T.base) {
-        const int2 e = stack[--T.sp];
-        if (st) st->nodes++;
-        if (__int_as_float(e.y) < T.r.MaxT) T.cur = e.x;
+        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+        if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
     if (!T.inProto) return true;
@@ -663,6 +690,10 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status,
     T.leafSlot = T.topSlot; T.leafLeft = T.topLeft;
     T.sp = T.base;
     T.base = 0;
+    if (T.leafLeft == 0) {
+        T.cur = PopNext(stack, &T.sp, 0, T.r.MaxT, st);
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+    }
     return false;
 }
 

@@ -324,6 +324,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     if (d->camera.width <= 0 || d->camera.height <= 0) throw RtFail(RT_ERR_INVALID_ARG, "scene: camera resolution must be positive");
     const int threads = std::max(1u, std::thread::hardware_concurrency());
     const int maxp = d->bvh_max_prims < 1 ? 1 : d->bvh_max_prims;
+    int tallest = 0;                           /* levels of the tallest tree */
 
     /* global vertex / triangle tables: every mesh, in mesh order */
     std::vector<float4> pos, nrm;
@@ -398,6 +399,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
             }
         }
         rtb::BuildResult br = rtb::build_sah(boxes, maxp, threads);
+        tallest = std::max(tallest, br.max_depth);
         emit_bvh(br, recs, nodes, slots, &bvhs[1 + b]);
         if (!br.nodes.empty()) blas_root[b] = br.nodes[0].bounds;
         else blas_root[b] = rtb::empty_box();
@@ -482,6 +484,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     }
     if (prims.empty()) throw RtFail(RT_ERR_INVALID_ARG, "scene: no primitives");
     rtb::BuildResult top = rtb::build_sah(boxes, maxp, threads);
+    tallest = std::max(tallest, top.max_depth);
     emit_bvh(top, recs, nodes, slots, &bvhs[0]);
 
     /* textures */
@@ -586,6 +589,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.light_count = (int)lights.size();
     v.infinite_count = (int)infinite.size();
     v.global_medium = d->global_medium < 0 ? -1 : d->global_medium;
+    v.deep_trees = tallest > RT_STACK_SIZE + 1 ? 1 : 0;
     RtCamera& cam = v.camera;
     cam.width = d->camera.width; cam.height = d->camera.height;
     cam.near_z = d->camera.near_z; cam.far_z = d->camera.far_z;

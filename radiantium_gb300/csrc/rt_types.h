@@ -155,7 +155,9 @@ struct RtSceneView {
     int32_t light_count;
     int32_t infinite_count;
     int32_t global_medium;
-    int32_t pad;
+    int32_t deep_trees;         /* a tree is taller than RT_STACK_SIZE + 1 levels: its
+                                 * traversal may overflow the stack, so every far child
+                                 * is pushed exactly as the reference pushes it */
     RtCamera camera;
 };
 
