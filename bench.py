@@ -155,9 +155,9 @@ def measured_peak():
 
 
 def profiled_traffic(name):
-    """Per-sample DRAM traffic of the path-tracing kernel from the committed ncu
-    summary (profiles/k_render_<workload>_traffic.txt: one line `bytes_per_sample=<x>`)."""
-    p = os.path.join(ROOT, "profiles", f"k_render_{name}_traffic.txt")
+    """Per-sample DRAM traffic of the traversal kernels from the committed ncu
+    summary (profiles/trace_<workload>_traffic.txt: one line `bytes_per_sample=<x>`)."""
+    p = os.path.join(ROOT, "profiles", f"trace_{name}_traffic.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -333,7 +333,7 @@ def run_ours(args):
     launch_ms = kernel_ms / max(1, render_launches)
     achieved = alg_bytes_step / (kernel_ms / args.steps / 1000.0) / 1e9
     peak, peak_src = measured_peak()
-    tps = profiled_traffic(args.workload)
+    tps = profiled_traffic(args.workload) if uses_wavefront else None
     traffic = None if tps is None else tps * samples_step / launches_per_step
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -351,7 +351,7 @@ def run_ours(args):
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
-                     "kernel": "k_wf_trace" if uses_wavefront else "k_render",
+                     "kernel": "k_wf_trace_closest + k_wf_trace_shadow" if uses_wavefront else "k_render",
                      "alg_bytes_per_launch": alg_bytes_step / launches_per_step, "launch_ms": launch_ms,
                      "launches_per_step": launches_per_step,
                      "kernel_ms_per_step": kernel_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
