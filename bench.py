@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront"], default="auto")
+    ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="steps of the plain megakernel timed in the same run for the batched/plain ratio (0: skip)")
     return ap.parse_args()
@@ -229,9 +229,10 @@ def run_ours(args):
     t0 = time.perf_counter()
     dev = Device(local)
     dev.upload(scene)
-    mode = {"auto": N.RENDERER_AUTO, "megakernel": N.RENDERER_MEGAKERNEL, "wavefront": N.RENDERER_WAVEFRONT}[args.renderer]
+    mode = {"auto": N.RENDERER_AUTO, "megakernel": N.RENDERER_MEGAKERNEL, "wavefront": N.RENDERER_WAVEFRONT,
+            "graph": N.RENDERER_WAVEFRONT_GRAPH}[args.renderer]
     dev.set_renderer(mode)
-    uses_wavefront = mode == N.RENDERER_WAVEFRONT or (
+    uses_wavefront = mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) or (
         mode == N.RENDERER_AUTO and st.integrator == N.INTEGRATOR_PATH and st.strategy == N.STRATEGY_UNIFORM)
     upload_s = time.perf_counter() - t0
     W, H = scene.camera.width, scene.camera.height

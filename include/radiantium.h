@@ -302,12 +302,36 @@ int rt_set_counting(void* ctx, int enabled);
 
 /* Selects the render pipeline: RT_RENDERER_AUTO (wavefront where it applies,
  * i.e. the `path` integrator with the Uniform light strategy; megakernel
- * otherwise), RT_RENDERER_MEGAKERNEL or RT_RENDERER_WAVEFRONT.  Both produce
- * identical films; this is the GpuWavefrontRenderer "renderer" option. */
+ * otherwise), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
+ * driven by the host, with per-phase timings in rt_stats) or
+ * RT_RENDERER_WAVEFRONT_GRAPH (bounce loop as one CUDA graph launch per
+ * round of samples).  All produce identical films; this is the
+ * GpuWavefrontRenderer "renderer" option. */
 #define RT_RENDERER_AUTO 0
 #define RT_RENDERER_MEGAKERNEL 1
 #define RT_RENDERER_WAVEFRONT 2
+#define RT_RENDERER_WAVEFRONT_GRAPH 3
 int rt_set_renderer(void* ctx, int mode);
+
+/* One render of a batch: the context holding its uploaded scene (may be the
+ * batch context itself), its parameters and its host output film (crop,
+ * ColorBuffer layout, width * height * 3 floats). */
+typedef struct rt_batch_item {
+    void* scene_ctx;
+    rt_render_params params;
+    float* out_rgb;
+} rt_batch_item;
+
+/* Renders n (1..256) scenes as one wavefront: their paths share one pool of
+ * path slots and every trace / shade launch, so small scenes do not leave
+ * the GPU idle and the launch overhead is paid once per bounce for the whole
+ * batch.  Each film equals what rt_render gives for the same item, bit for
+ * bit.  Every item must use the `path` integrator with the Uniform light
+ * strategy, and all scene contexts must be on the batch context's device.
+ * The bounce loop runs as a CUDA graph unless rt_set_renderer selected
+ * RT_RENDERER_WAVEFRONT.  No counterpart in the reference, which renders one
+ * scene per process (Radiantium.Cli/Program.cs). */
+int rt_render_batch(void* ctx, const rt_batch_item* items, int n);
 
 /* Requests cancellation of a running render (Renderer.Stop, BlockBasedRenderer.cs:85-88). */
 int rt_cancel(void* ctx);

@@ -78,9 +78,16 @@ struct Ctx {
     WfState wf{};
     std::vector<DevBuf> wf_bufs;
     int wf_slots = 0;
-    int32_t* wf_counters = nullptr;            /* [0] rays queued, [1] / [2] active lists, [3] shadow rays, [4] / [5] fetch */
-    int32_t* h_counts = nullptr;               /* pinned mirror of wf_counters */
-    int wf_capacity = 1 << 21;                 /* path slots in flight */
+    WfCounters* d_ctr = nullptr;               /* device counters of a wavefront run */
+    WfCounters* h_ctr = nullptr;               /* pinned staging / mirror of d_ctr */
+    WfJob* d_jobs = nullptr;                   /* device job table (WF_MAX_JOBS entries) */
+    WfJob* h_jobs = nullptr;                   /* pinned staging of the job table */
+    int wf_capacity = WF_MAX_SLOTS;            /* path slots in flight */
+    uint64_t wf_generation = 0;                /* bumped whenever the path-state buffers move */
+    /* the bounce loop captured as a CUDA graph while-loop */
+    cudaGraph_t wf_graph = nullptr;
+    cudaGraphExec_t wf_exec = nullptr;
+    uint64_t wf_graph_key = 0;                 /* generation, slots and counting it was built for */
 };
 
 void ensure_events(Ctx* c, size_t n) {
@@ -144,10 +151,9 @@ void ensure_wf(Ctx* c, int slots) {
     WfState& W = c->wf;
     const size_t n = (size_t)slots, q = 3 * (size_t)slots;
     W.q_o = wf_alloc<float4>(c, q); W.q_d = wf_alloc<float4>(c, q); W.q_meta = wf_alloc<int32_t>(c, q);
-    W.active = wf_alloc<int32_t>(c, n); W.active_next = wf_alloc<int32_t>(c, n);
+    W.active[0] = wf_alloc<int32_t>(c, n); W.active[1] = wf_alloc<int32_t>(c, n);
     W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint8_t>(c, n);
-    W.key_count = wf_alloc<int32_t>(c, 32);
-    W.next_sample = wf_alloc<unsigned long long>(c, 1);
+    W.job = wf_alloc<uint8_t>(c, n);
     W.pix = wf_alloc<int4>(c, n); W.rng_n = wf_alloc<uint32_t>(c, n);
     W.coeff = wf_alloc<float4>(c, n); W.rad = wf_alloc<float4>(c, n);
     W.bounce = wf_alloc<int2>(c, n); W.flags = wf_alloc<uint32_t>(c, n);
@@ -158,9 +164,14 @@ void ensure_wf(Ctx* c, int slots) {
     W.ext_hit = wf_alloc<float4>(c, n); W.ext_sub = wf_alloc<int32_t>(c, n);
     W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
     W.occluded = wf_alloc<uint8_t>(c, n);
-    if (!c->wf_counters) CK(cudaMalloc((void**)&c->wf_counters, 8 * sizeof(int32_t)));
-    if (!c->h_counts) CK(cudaMallocHost((void**)&c->h_counts, 4 * sizeof(int32_t)));
+    if (!c->d_ctr) CK(cudaMalloc((void**)&c->d_ctr, sizeof(WfCounters)));
+    if (!c->h_ctr) CK(cudaMallocHost((void**)&c->h_ctr, sizeof(WfCounters)));
+    if (!c->d_jobs) CK(cudaMalloc((void**)&c->d_jobs, WF_MAX_JOBS * sizeof(WfJob)));
+    if (!c->h_jobs) CK(cudaMallocHost((void**)&c->h_jobs, WF_MAX_JOBS * sizeof(WfJob)));
+    W.ctr = c->d_ctr;
+    W.jobs = c->d_jobs;
     c->wf_slots = slots;
+    c->wf_generation++;
 }
 
 /* ---- host float helpers with the kernels' operation order --------------- */
@@ -645,9 +656,10 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
     const bool uniform_path = P.integrator == RT_INTEGRATOR_PATH && P.strategy == RT_STRATEGY_UNIFORM;
-    if (c->renderer == RT_RENDERER_WAVEFRONT && !uniform_path)
+    const bool wavefront = c->renderer == RT_RENDERER_WAVEFRONT || c->renderer == RT_RENDERER_WAVEFRONT_GRAPH;
+    if (wavefront && !uniform_path)
         throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs the path integrator with the Uniform light strategy");
-    if (c->renderer == RT_RENDERER_WAVEFRONT || (c->renderer == RT_RENDERER_AUTO && uniform_path)) {
+    if (wavefront || (c->renderer == RT_RENDERER_AUTO && uniform_path)) {
         render_wavefront(c, P, chunk, npix, s);
     } else {
         render_megakernel(c, P, chunk, npix, s);
@@ -759,67 +771,212 @@ void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t 
     if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
 }
 
-/* wavefront: trace all queued rays, shade all active paths, repeat until
- * every sample of the chunk has finished (rt_wavefront.cu) */
-void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
-    const int64_t max_samples = npix * (int64_t)chunk;
-    const int slots = (int)std::min<int64_t>(c->wf_capacity, max_samples + 31);
-    ensure_wf(c, slots);
+/* one render of a wavefront run: scene, parameters (full spp), film sums */
+struct WfJobIn {
+    const RtSceneView* view;
+    RtParams P;
+    float* film;
+};
+
+/* The bounce loop as a graph: a while node whose body is one iteration
+ * (trace, phase, sort, shade, tail); the tail kernel clears the loop's
+ * condition when no path is left.  Rebuilt when the path state moves or the
+ * counting mode changes. */
+void ensure_wf_graph(Ctx* c, const WfState& W) {
+    const uint64_t key = (c->wf_generation << 24) ^ ((uint64_t)W.slots << 1) ^ (c->counting ? 1u : 0u);
+    if (c->wf_exec && c->wf_graph_key == key) return;
+    if (c->wf_exec) { cudaGraphExecDestroy(c->wf_exec); c->wf_exec = nullptr; }
+    if (c->wf_graph) { cudaGraphDestroy(c->wf_graph); c->wf_graph = nullptr; }
+    CK(cudaGraphCreate(&c->wf_graph, 0));
+    cudaGraphConditionalHandle loop;
+    CK(cudaGraphConditionalHandleCreate(&loop, c->wf_graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, c->wf_graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    uint64_t launches = 0;
+    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream);
+    cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches);
+    cudaGraph_t captured = nullptr;
+    CK(cudaStreamEndCapture(c->stream, &captured));
+    CK(e1);
+    CK(e2);
+    CK(cudaGraphInstantiate(&c->wf_exec, c->wf_graph, 0));
+    c->wf_graph_key = key;
+}
+
+/* Renders every job: rounds of up to sample_budget samples (each job gets
+ * the same number of sample indices per round); within a round all jobs'
+ * paths share the path slots, queues and launches (rt_wavefront.cu).  The
+ * bounce loop is driven from the host (per-phase timing) or, with
+ * `use_graph`, runs as one CUDA graph launch per round. */
+void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, bool use_graph) {
+    if (jobs.empty() || jobs.size() > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "wavefront: 1 to 256 jobs per run");
+    std::vector<int> done(jobs.size(), 0);
     ensure_events(c, 4);
-    WfState W = c->wf;
-    W.samples = c->samples;
-    W.n_rays_next = c->wf_counters;
-    W.n_shadow_next = c->wf_counters + 3;
-    W.shadow_base = 2 * slots;
-    W.fetch = c->wf_counters + 4;
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
-    for (int b = 0; b < P.spp; b += chunk) {
+    while (true) {
         if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-        P.chunk_begin = b;
-        P.chunk_len = std::min(chunk, P.spp - b);
-        W.n_active = c->wf_counters + 1;
-        W.n_active_next = c->wf_counters + 2;
-        W.active = c->wf.active;
-        W.active_next = c->wf.active_next;
-        CK(cudaMemsetAsync(c->wf_counters, 0, 4 * sizeof(int32_t), s));
-        CK(cudaMemsetAsync(W.next_sample, 0, sizeof(unsigned long long), s));
-        CK(rt_wf_start(c->d_view, P, W, slots, s));
-        launches += 2;
-        CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        int n_rays = c->h_counts[0], n_active = c->h_counts[1], n_shadow = c->h_counts[3];
-        while (n_active > 0) {
-            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-            CK(cudaEventRecord(c->events[0], s));
-            CK(rt_wf_trace(c->d_view, W, n_rays, n_shadow, c->status, c->stats, c->counting, s));
-            CK(cudaEventRecord(c->events[1], s));
-            CK(cudaMemsetAsync(W.n_rays_next, 0, sizeof(int32_t), s));
-            CK(cudaMemsetAsync(W.n_shadow_next, 0, sizeof(int32_t), s));
-            CK(cudaMemsetAsync(W.n_active_next, 0, sizeof(int32_t), s));
-            CK(cudaEventRecord(c->events[2], s));
-            CK(rt_wf_shade(c->d_view, P, W, n_active, c->status, c->stats, c->counting, true, s, &launches));
-            CK(cudaEventRecord(c->events[3], s));
-            launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0);
-            trace_launches += (n_rays > 0 ? 1 : 0) + (n_shadow > 0 ? 1 : 0);
-            std::swap(W.active, W.active_next);
-            std::swap(W.n_active, W.n_active_next);
-            CK(cudaMemcpyAsync(c->h_counts, c->wf_counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            n_rays = c->h_counts[0];
-            n_shadow = c->h_counts[3];
-            n_active = c->h_counts[W.n_active - c->wf_counters];
-            float t = 0;
-            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
-            CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+        std::vector<int> act;
+        int64_t npix_total = 0;
+        for (size_t j = 0; j < jobs.size(); j++)
+            if (done[j] < jobs[j].P.spp) { act.push_back((int)j); npix_total += (int64_t)jobs[j].P.w * jobs[j].P.h; }
+        if (act.empty()) break;
+        const int64_t chunk = std::max<int64_t>(1, c->sample_budget / npix_total);
+        int64_t total = 0;
+        std::vector<int> clen(act.size());
+        for (size_t k = 0; k < act.size(); k++) {
+            const WfJobIn& J = jobs[act[k]];
+            clen[k] = (int)std::min<int64_t>(chunk, J.P.spp - done[act[k]]);
+            total += (int64_t)J.P.w * J.P.h * clen[k];
         }
-        CK(rt_launch_accumulate(c->film, c->samples, npix, P.chunk_len, s));
-        launches += 1;
+        ensure(&c->samples, &c->samples_bytes, (size_t)total * 12);
+        const int slots = (int)std::min<int64_t>(std::min<int64_t>(c->wf_capacity, WF_MAX_SLOTS), total + 31);
+        ensure_wf(c, slots);
+        CK(cudaStreamSynchronize(s));          /* the pinned staging of the last round has been read */
+        int64_t first = 0;
+        for (size_t k = 0; k < act.size(); k++) {
+            const WfJobIn& J = jobs[act[k]];
+            WfJob& d = c->h_jobs[k];
+            d.view = J.view;
+            d.P = J.P;
+            d.P.chunk_begin = done[act[k]];
+            d.P.chunk_len = clen[k];
+            d.samples = c->samples + first * 3;
+            d.first = first;
+            d.count = (int64_t)J.P.w * J.P.h * clen[k];
+            first += d.count;
+        }
+        std::memset(c->h_ctr, 0, sizeof(WfCounters));
+        c->h_ctr->total = total;
+        c->h_ctr->n_jobs = (int)act.size();
+        CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, act.size() * sizeof(WfJob), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+        WfState W = c->wf;
+        W.slots = slots;
+        W.shadow_base = 2 * slots;
+        CK(rt_wf_start(W, s));
+        launches += 2;
+        if (use_graph) {
+            ensure_wf_graph(c, W);
+            CK(cudaEventRecord(c->events[0], s));
+            CK(cudaGraphLaunch(c->wf_exec, s));
+            CK(cudaEventRecord(c->events[1], s));
+            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
+            launches += 7 * iters;
+            trace_launches += 2 * iters;
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
+            trace_ms += t;                      /* the whole loop: not split by phase */
+        } else {
+            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0) {
+                if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+                if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+                CK(cudaEventRecord(c->events[0], s));
+                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+                CK(cudaEventRecord(c->events[1], s));
+                CK(cudaEventRecord(c->events[2], s));
+                CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
+                               s, &launches));
+                CK(cudaEventRecord(c->events[3], s));
+                launches += 2;
+                trace_launches += 2;
+                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                float t = 0;
+                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
+                CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+            }
+        }
+        for (size_t k = 0; k < act.size(); k++) {
+            const WfJobIn& J = jobs[act[k]];
+            CK(rt_launch_accumulate(J.film, c->h_jobs[k].samples, (int64_t)J.P.w * J.P.h, clen[k], s));
+            launches += 1;
+            done[act[k]] += clen[k];
+        }
     }
     c->last.render_kernel_ms = trace_ms;
     c->last.shade_kernel_ms = shade_ms;
     c->last.render_launches = trace_launches;
     c->last.kernel_launches = launches;
+}
+
+void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
+    (void)chunk; (void)npix;
+    std::vector<WfJobIn> jobs(1);
+    jobs[0].view = c->d_view;
+    jobs[0].P = P;
+    jobs[0].film = c->film;
+    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH);
+}
+
+/* rt_render_batch: every item's film through one wavefront run */
+void render_batch(Ctx* c, const rt_batch_item* items, int n) {
+    if (!items || n <= 0 || n > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: 1 to 256 items");
+    std::vector<WfJobIn> jobs((size_t)n);
+    std::vector<int64_t> film_off((size_t)n);
+    int64_t film_floats = 0;
+    for (int i = 0; i < n; i++) {
+        const rt_batch_item& it = items[i];
+        Ctx* sc = (Ctx*)it.scene_ctx;
+        const rt_render_params* p = &it.params;
+        if (!sc || !it.out_rgb) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " has no scene context or output");
+        if (sc->device != c->device) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " is on another device");
+        if (!sc->has_scene) throw RtFail(RT_ERR_NO_SCENE, "render_batch: item " + std::to_string(i) + " has no uploaded scene");
+        if (p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " has spp <= 0");
+        if (p->integrator != RT_INTEGRATOR_PATH || p->strategy != RT_STRATEGY_UNIFORM)
+            throw RtFail(RT_ERR_UNSUPPORTED, "render_batch: items must use the path integrator with the Uniform light strategy");
+        RtParams P{};
+        P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
+        P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;
+        P.seed = p->seed; P.x0 = p->x0; P.y0 = p->y0;
+        P.w = p->width > 0 ? p->width : sc->width - p->x0;
+        P.h = p->height > 0 ? p->height : sc->height - p->y0;
+        if (P.x0 < 0 || P.y0 < 0 || P.w <= 0 || P.h <= 0 || P.x0 + P.w > sc->width || P.y0 + P.h > sc->height)
+            throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " crop outside the film");
+        P.spp = p->spp; P.sample_begin = p->sample_begin;
+        jobs[i].view = sc->d_view;
+        jobs[i].P = P;
+        film_off[i] = film_floats;
+        film_floats += (int64_t)P.w * P.h * 3;
+    }
+    cudaStream_t s = c->stream;
+    ensure(&c->film, &c->film_bytes, (size_t)film_floats * 4);
+    ensure(&c->out, &c->out_bytes, (size_t)film_floats * 4);
+    for (int i = 0; i < n; i++) jobs[i].film = c->film + film_off[i];
+    CK(cudaMemsetAsync(c->film, 0, (size_t)film_floats * 4, s));
+    CK(cudaMemsetAsync(c->status, 0, 4, s));
+    CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
+    c->cancel.store(0);
+    wavefront_run(c, jobs, s, c->renderer != RT_RENDERER_WAVEFRONT);
+    uint64_t samples = 0;
+    for (int i = 0; i < n; i++) {
+        const int64_t npix = (int64_t)jobs[i].P.w * jobs[i].P.h;
+        CK(rt_launch_finalize(c->out + film_off[i], c->film + film_off[i], npix, (float)jobs[i].P.spp, s));
+        CK(cudaMemcpyAsync(items[i].out_rgb, c->out + film_off[i], (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
+        samples += (uint64_t)npix * jobs[i].P.spp;
+    }
+    CK(cudaStreamSynchronize(s));
+    check_status(c);
+    double rms = c->last.render_kernel_ms, sms = c->last.shade_kernel_ms;
+    uint64_t launches = c->last.kernel_launches, rl = c->last.render_launches;
+    std::memset(&c->last, 0, sizeof(c->last));
+    read_stats(c);
+    c->last.samples = samples;
+    c->last.render_kernel_ms = rms;
+    c->last.shade_kernel_ms = sms;
+    c->last.render_launches = rl;
+    c->last.kernel_launches = launches + (uint64_t)n;
 }
 
 void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
@@ -907,8 +1064,12 @@ void rt_destroy(void* ctx) {
     if (c->status) cudaFree(c->status);
     if (c->stats) cudaFree(c->stats);
     free_wf(c);
-    if (c->wf_counters) cudaFree(c->wf_counters);
-    if (c->h_counts) cudaFreeHost(c->h_counts);
+    if (c->wf_exec) cudaGraphExecDestroy(c->wf_exec);
+    if (c->wf_graph) cudaGraphDestroy(c->wf_graph);
+    if (c->d_ctr) cudaFree(c->d_ctr);
+    if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    if (c->d_jobs) cudaFree(c->d_jobs);
+    if (c->h_jobs) cudaFreeHost(c->h_jobs);
     for (cudaEvent_t e : c->events) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -948,6 +1109,10 @@ int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render(c, params, d_out_rgb, false, (cudaStream_t)stream); });
 }
+int rt_render_batch(void* ctx, const rt_batch_item* items, int n) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render_batch(c, items, n); });
+}
 int rt_render_device_noalloc(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render_noalloc(c, params, d_out_rgb, (cudaStream_t)stream); });
@@ -966,7 +1131,7 @@ int rt_set_counting(void* ctx, int enabled) {
 }
 int rt_set_renderer(void* ctx, int mode) {
     Ctx* c = (Ctx*)ctx;
-    if (!c || mode < RT_RENDERER_AUTO || mode > RT_RENDERER_WAVEFRONT) return RT_ERR_INVALID_ARG;
+    if (!c || mode < RT_RENDERER_AUTO || mode > RT_RENDERER_WAVEFRONT_GRAPH) return RT_ERR_INVALID_ARG;
     c->renderer = mode;
     return RT_OK;
 }
@@ -981,6 +1146,17 @@ int rt_cancel(void* ctx) {
  * boxes (6 floats each) on the host exactly as rt_upload_scene does and
  * returns it in depth-first LinearBVHNode form.  Call with null arrays to get
  * the node count.  No CUDA call is made. */
+/* test hook (not in the public header): shrinks the samples per round and
+ * the path slots in flight so small renders exercise several rounds and
+ * heavy slot reuse; 0 keeps a value */
+int rt_debug_set_limits(void* ctx, int64_t sample_budget, int wf_capacity) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || sample_budget < 0 || wf_capacity < 0) return RT_ERR_INVALID_ARG;
+    if (sample_budget > 0) c->sample_budget = sample_budget;
+    if (wf_capacity > 0) c->wf_capacity = std::min(wf_capacity, WF_MAX_SLOTS);
+    return RT_OK;
+}
+
 int rt_debug_bvh(const float* boxes, int n, int max_prims, int64_t* node_count, float* bounds, int32_t* idx,
                  int32_t* count, int32_t* axis, int32_t* order) {
     if (!boxes || n <= 0 || !node_count) return RT_ERR_INVALID_ARG;

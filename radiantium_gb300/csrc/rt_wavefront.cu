@@ -22,6 +22,13 @@
  * bounce b+1), so every sample is bit-identical to the megakernel and to the
  * CPU oracle.  Path slots whose path has finished are refilled with the next
  * camera sample, which keeps the queues full to the end of a render.
+ *
+ * A run renders a batch of jobs (rt_wavefront.h): a path slot records its
+ * job, and the scene view and parameters of that job drive its traversal and
+ * shading, so paths of every scene of a batch share one set of launches.
+ * Every launch reads its work count from device memory and the active lists
+ * alternate by iteration parity, so the launch sequence of one bounce never
+ * changes and can be captured into a CUDA graph loop.
  */
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -64,7 +71,20 @@ DF int warp_append(int* counter, bool want) {
 DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
     W.q_o[q] = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
     W.q_d[q] = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
-    W.q_meta[q] = (path << 2) | kind;
+    W.q_meta[q] = (path << 10) | ((int)W.job[path] << 2) | kind;
+}
+DF int meta_path(int meta) { return meta >> 10; }
+DF int meta_job(int meta) { return (meta >> 2) & (WF_MAX_JOBS - 1); }
+DF int meta_kind(int meta) { return meta & 3; }
+
+/* job of a batch-wide sample id (jobs are ordered by their first id) */
+DF int job_of(const WfState& W, long long sid) {
+    int lo = 0, hi = W.ctr->n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (W.jobs[mid].first <= sid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 /* Rng resumed at draw n of its stream */
@@ -90,28 +110,32 @@ DF void sample_pixel(const RtParams& P, int64_t sid, int* lx, int* ly, int* k) {
 
 /* initialises a camera sample in `slot` and enqueues its first ray; the
  * warp claims its sample ids with one atomic.  Returns false (slot emptied)
- * when every sample of the chunk has been started. */
-DF bool start_path(const RtSceneView* S, const RtParams& P, const WfState& W, int slot, bool take) {
-    const int64_t total = (int64_t)P.w * P.h * P.chunk_len;
+ * when every sample of the round has been started. */
+DF bool start_path(const WfState& W, int slot, bool take) {
+    const long long total = W.ctr->total;
     unsigned mask = __ballot_sync(__activemask(), take);
-    int64_t sid = -1;
+    long long sid = -1;
     if (take) {
         int leader = __ffs(mask) - 1, lane = threadIdx.x & 31;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(W.next_sample, (unsigned long long)__popc(mask));
+        if (lane == leader) base = atomicAdd(&W.ctr->next_sample, (unsigned long long)__popc(mask));
         base = __shfl_sync(mask, base, leader);
-        int64_t id = (int64_t)base + __popc(mask & ((1u << lane) - 1u));
+        long long id = (long long)base + __popc(mask & ((1u << lane) - 1u));
         if (id < total) sid = id;
     }
-    int q = warp_append(W.n_rays_next, sid >= 0);
+    int q = warp_append(&W.ctr->n_closest, sid >= 0);
     if (sid < 0) { W.flags[slot] = 0; return false; }
+    const int j = job_of(W, sid);
+    const WfJob& J = W.jobs[j];
+    const RtParams P = J.P;
+    W.job[slot] = (uint8_t)j;
     int lx, ly, k;
-    sample_pixel(P, sid, &lx, &ly, &k);
+    sample_pixel(P, sid - J.first, &lx, &ly, &k);
     int px = P.x0 + lx, py = P.y0 + ly, t = P.sample_begin + P.chunk_begin + k;
     Rng rand;
     rng_init(rand, P.seed, (uint32_t)px, (uint32_t)py, (uint32_t)t);
     V2 jit = NextVec2(rand);
-    Ray ray = CameraRay(S->camera, v2((float)px + jit.x, (float)py + jit.y));
+    Ray ray = CameraRay(J.view->camera, v2((float)px + jit.x, (float)py + jit.y));
     W.pix[slot] = make_int4(lx, ly, k, t);
     W.rng_n[slot] = rand.n;
     W.coeff[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
@@ -124,10 +148,10 @@ DF bool start_path(const RtSceneView* S, const RtParams& P, const WfState& W, in
     return true;
 }
 
-__global__ void __launch_bounds__(256) k_wf_start(const RtSceneView* __restrict__ S, RtParams P, WfState W, int slots) {
+__global__ void __launch_bounds__(256) k_wf_start(WfState W) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= slots) return;
-    start_path(S, P, W, slot, true);
+    if (slot >= W.slots) return;
+    start_path(W, slot, true);
 }
 
 /* Persistent traversal with dynamic ray fetch (Aila & Laine 2009): each warp
@@ -155,36 +179,39 @@ DF Ray queued_ray(const WfState& W, int q) {
     return mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w, d.w);
 }
 
-DF void closest_done(const WfState& W, int q, const TravClosest& T) {
-    const int meta = W.q_meta[q];
-    const int path = meta >> 2;
+DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
+    const int path = meta_path(meta);
     const float4 h = make_float4(T.best.t, T.best.u, T.best.v, __int_as_float(T.any ? T.best.slot : -1));
-    if ((meta & 3) == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = T.best.sub; }
+    if (meta_kind(meta) == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = T.best.sub; }
     else { W.mis_hit[path] = h; W.mis_sub[path] = T.best.sub; }
 }
 
-/* closest-hit rays: extension and MIS rays (queue [0, n)) */
-__global__ void __launch_bounds__(128) k_wf_trace_closest(const RtSceneView* __restrict__ S, WfState W, int n,
-                                                            uint32_t* status, unsigned long long* stats, bool counting) {
+/* closest-hit rays: extension and MIS rays (queue [0, n_closest)) */
+__global__ void __launch_bounds__(128) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
+                                                            bool counting) {
+    const int n = min(W.ctr->n_closest, 2 * W.slots);
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
     TravStats* pst = counting ? &st : nullptr;
     uint32_t done = 0;
     TravClosest T;
-    int item = -1;
+    const RtSceneView* S = nullptr;
+    int item = -1, meta = 0;
     bool exhausted = false;
     while (true) {
         const unsigned idle = __ballot_sync(kFullWarp, item < 0);
         if (exhausted) {
             if (idle == kFullWarp) break;
         } else if (__popc(idle) >= kRefill) {
-            const int q = fetch_entry(W.fetch, n, idle, &exhausted);
+            const int q = fetch_entry(&W.ctr->fetch[0], n, idle, &exhausted);
             if (item < 0 && q < n) {
-                if (ClosestBegin(S, queued_ray(W, q), T, pst)) { closest_done(W, q, T); done++; }
+                meta = W.q_meta[q];
+                S = W.jobs[meta_job(meta)].view;
+                if (ClosestBegin(S, queued_ray(W, q), T, pst)) { closest_done(W, meta, T); done++; }
                 else item = q;
             }
         }
-        if (item >= 0 && ClosestStep(S, T, stack, status, pst)) { closest_done(W, item, T); done++; item = -1; }
+        if (item >= 0 && ClosestStep(S, T, stack, status, pst)) { closest_done(W, meta, T); done++; item = -1; }
     }
     if (counting) {
         warp_add64(stats + 1, done);
@@ -194,30 +221,35 @@ __global__ void __launch_bounds__(128) k_wf_trace_closest(const RtSceneView* __r
     }
 }
 
-/* shadow rays: any-hit (queue [shadow_base, shadow_base + n)) */
-__global__ void __launch_bounds__(128) k_wf_trace_shadow(const RtSceneView* __restrict__ S, WfState W, int n,
-                                                           uint32_t* status, unsigned long long* stats, bool counting) {
+/* shadow rays: any-hit (queue [shadow_base, shadow_base + n_shadow)) */
+__global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t* status, unsigned long long* stats,
+                                                           bool counting) {
+    const int n = min(W.ctr->n_shadow, W.slots);
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
     TravStats* pst = counting ? &st : nullptr;
     uint32_t done = 0;
     TravAny T;
-    int item = -1;
+    const RtSceneView* S = nullptr;
+    int item = -1, path = 0;
     bool exhausted = false;
     while (true) {
         const unsigned idle = __ballot_sync(kFullWarp, item < 0);
         if (exhausted) {
             if (idle == kFullWarp) break;
         } else if (__popc(idle) >= kRefill) {
-            const int e = fetch_entry(W.fetch + 1, n, idle, &exhausted);
+            const int e = fetch_entry(&W.ctr->fetch[1], n, idle, &exhausted);
             if (item < 0 && e < n) {
                 const int q = W.shadow_base + e;
-                if (AnyBegin(S, queued_ray(W, q), T, pst)) { W.occluded[W.q_meta[q] >> 2] = 0; done++; }
+                const int meta = W.q_meta[q];
+                path = meta_path(meta);
+                S = W.jobs[meta_job(meta)].view;
+                if (AnyBegin(S, queued_ray(W, q), T, pst)) { W.occluded[path] = 0; done++; }
                 else item = q;
             }
         }
         if (item >= 0 && AnyStep(S, T, stack, status, pst)) {
-            W.occluded[W.q_meta[item] >> 2] = T.hit ? 1 : 0;
+            W.occluded[path] = T.hit ? 1 : 0;
             done++;
             item = -1;
         }
@@ -265,23 +297,22 @@ DF bool load_hit(const RtSceneView* S, const Ray& ray, float4 h, int sub, Isect*
     return true;
 }
 
-DF void finish_path(const RtParams& P, const WfState& W, int slot, C3 rad, unsigned long long* stats) {
+DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned long long* stats) {
     bool invalid = !IsValid(rad);
     if (invalid) { rad = c3s(0.0f); atomicAdd(stats + 6, 1ull); }
     int4 px = W.pix[slot];
+    const RtParams& P = J.P;
     const int64_t npix = (int64_t)P.w * P.h;
-    float* o = W.samples + ((int64_t)px.z * npix + (int64_t)px.x * P.h + px.y) * 3;
+    float* o = J.samples + ((int64_t)px.z * npix + (int64_t)px.x * P.h + px.y) * 3;
     o[0] = rad.r; o[1] = rad.g; o[2] = rad.b;
 }
 
 /* one bounce of PathTracer.Mis / NextEventEstimation / OnlySampleBxdf after the
  * extension hit is known (PathTracer.cs:43-270) */
-__global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict__ S, RtParams P, WfState W, int n,
-                                                    uint32_t* status, unsigned long long* stats, bool counting,
-                                                    bool regenerate) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int slot = W.active[i];
+DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting) {
+    const WfJob& J = W.jobs[W.job[slot]];
+    const RtSceneView* S = J.view;
+    const RtParams P = J.P;                  /* registers: the path-state stores below cannot alias it */
     uint32_t fl = W.flags[slot];
     float4 cf = W.coeff[slot], rd = W.rad[slot];
     C3 coeff = c3(cf.x, cf.y, cf.z), radiance = c3(rd.x, rd.y, rd.z);
@@ -380,7 +411,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
                                     C3 l1 = fr * ls.Li * weight / ls.Pdf;
                                     W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
                                     fl |= F_L1;
-                                    int q = W.shadow_base + warp_append(W.n_shadow_next, true);
+                                    int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
                                     push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
                                 }
                             }
@@ -406,7 +437,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
                                 W.pd_ray_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
                                 W.pd_ray_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, toLight.MaxT);
                                 fl |= F_L2;
-                                int q = warp_append(W.n_rays_next, true);
+                                int q = warp_append(&W.ctr->n_closest, true);
                                 push_ray(W, q, slot, WF_RAY_MIS, toLight);
                             }
                         }
@@ -427,7 +458,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
                                 C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
                                 W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
                                 zero = false;
-                                int q = W.shadow_base + warp_append(W.n_shadow_next, true);
+                                int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
                                 push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
                             }
                         }
@@ -450,7 +481,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
             ext = true;
         } while (false);
         if (ext) {
-            int q = warp_append(W.n_rays_next, true);
+            int q = warp_append(&W.ctr->n_closest, true);
             push_ray(W, q, slot, WF_RAY_EXT, nray);
             W.ray_o[slot] = make_float4(nray.O.x, nray.O.y, nray.O.z, nray.MinT);
             W.ray_d[slot] = make_float4(nray.D.x, nray.D.y, nray.D.z, nray.MaxT);
@@ -463,131 +494,158 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RtSceneView* __restrict_
     W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0);
     W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0);
     /* the slot stays active while it waits for rays */
-    if (fl & F_PENDING) {
+    if ((fl & F_PENDING) || !(fl & F_DONE)) {
         W.flags[slot] = fl;
-        int a = warp_append(W.n_active_next, true);
-        W.active_next[a] = slot;
+        int a = warp_append(&W.ctr->n_active[next], true);
+        W.active[next][a] = slot;
         return;
     }
-    if (!(fl & F_DONE)) {
-        W.flags[slot] = fl;
-        int a = warp_append(W.n_active_next, true);
-        W.active_next[a] = slot;
-        return;
-    }
-    finish_path(P, W, slot, radiance, stats);
+    finish_path(J, W, slot, radiance, stats);
     if (counting) warp_add64(stats + 0, 1u);
-    if (regenerate && start_path(S, P, W, slot, true)) {
-        int a = warp_append(W.n_active_next, true);
-        W.active_next[a] = slot;
+    if (start_path(W, slot, true)) {
+        int a = warp_append(&W.ctr->n_active[next], true);
+        W.active[next][a] = slot;
     } else {
         W.flags[slot] = 0;
-        warp_append(W.n_active_next, false);
+        warp_append(&W.ctr->n_active[next], false);
     }
 }
 
-__global__ void k_wf_active_init(WfState W, int slots) {
+/* the active paths of this iteration, one thread each over the sorted list;
+ * the grid covers every slot and the blocks past the active count return */
+__global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting) {
+    const int cur = W.ctr->iter & 1;
+    const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= slots) return;
+    if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+}
+
+__global__ void k_wf_active_init(WfState W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W.slots) return;
     bool alive = (W.flags[i] & F_ALIVE) != 0;
-    int a = warp_append(W.n_active, alive);
-    if (alive) W.active[a] = i;
-}
-
-inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
-
-}  // namespace
-
-cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& W, int slots, cudaStream_t s) {
-    k_wf_start<<<grid_for(slots, 256), 256, 0, s>>>(S, P, W, slots);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_wf_active_init<<<grid_for(slots, 256), 256, 0, s>>>(W, slots);
-    return cudaGetLastError();
-}
-
-/* resident blocks of a persistent trace kernel: every SM filled once */
-template <typename K>
-int persistent_blocks(K kernel, int n) {
-    int dev = 0, sms = 0, per_sm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess || per_sm <= 0)
-        per_sm = 1, sms = sms > 0 ? sms : 1;
-    const int64_t need = ((int64_t)n + 127) / 128;
-    return (int)std::min<int64_t>(need, (int64_t)sms * per_sm);
-}
-
-cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
-                        unsigned long long* stats, bool counting, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(W.fetch, 0, 2 * sizeof(int32_t), s);
-    if (e != cudaSuccess) return e;
-    if (n_closest > 0)
-        k_wf_trace_closest<<<persistent_blocks(k_wf_trace_closest, n_closest), 128, 0, s>>>(S, W, n_closest, status, stats, counting);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    if (n_shadow > 0)
-        k_wf_trace_shadow<<<persistent_blocks(k_wf_trace_shadow, n_shadow), 128, 0, s>>>(S, W, n_shadow, status, stats, counting);
-    return cudaGetLastError();
+    int a = warp_append(&W.ctr->n_active[0], alive);
+    if (alive) W.active[0][a] = i;
 }
 
 /* Shade key of an active path: which code the shade kernel will run for it.
  * 0 finished (pending term, then a new sample), 1 missed the scene, 2 hit a
  * medium boundary without a surface, 3 + RT_MAT_* hit that material type. */
-constexpr int kShadeKeys = 16;
-DF int shade_key(const RtSceneView* S, const WfState& W, int slot) {
+DF int shade_key(const WfState& W, int slot) {
     if (W.flags[slot] & F_DONE) return 0;
     const int hs = __float_as_int(W.ext_hit[slot].w);
     if (hs < 0) return 1;
+    const RtSceneView* S = W.jobs[W.job[slot]].view;
     const int prim = __float_as_int(__ldg(S->slots + 3 * (int64_t)hs).w);
     const int m = S->prims[prim].material;
     if (m < 0) return 2;
-    return min(3 + S->materials[m].type, kShadeKeys - 1);
+    return min(3 + S->materials[m].type, WF_SHADE_KEYS - 1);
 }
 
-__global__ void __launch_bounds__(256) k_wf_sort_count(const RtSceneView* __restrict__ S, WfState W, int n) {
+/* between trace and shade: the queues are consumed, reset their counters */
+__global__ void k_wf_phase(WfState W) {
+    if (threadIdx.x == 0) {
+        WfCounters* c = W.ctr;
+        c->n_closest = 0; c->n_shadow = 0; c->fetch[0] = 0; c->fetch[1] = 0;
+        c->n_active[(c->iter & 1) ^ 1] = 0;
+    }
+    if (threadIdx.x < 2 * WF_SHADE_KEYS) W.ctr->key_count[threadIdx.x] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_wf_sort_count(WfState W) {
+    const int cur = W.ctr->iter & 1;
+    const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int key = shade_key(S, W, W.active[i]);
+    const int key = shade_key(W, W.active[cur][i]);
     W.sort_key[i] = (uint8_t)key;
     const unsigned peers = __match_any_sync(__activemask(), key);
-    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.key_count + key, __popc(peers));
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.ctr->key_count + key, __popc(peers));
 }
 
 /* counting-sort scatter: entries of one key stay together, in any order
  * (every path's result is independent of the order paths are shaded in) */
-__global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W, int n) {
-    __shared__ int base[kShadeKeys];
-    if (threadIdx.x < kShadeKeys) {
+__global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
+    __shared__ int base[WF_SHADE_KEYS];
+    const int cur = W.ctr->iter & 1;
+    const int n = min(W.ctr->n_active[cur], W.slots);
+    if ((int)(blockIdx.x * blockDim.x) >= n) return;
+    if (threadIdx.x < WF_SHADE_KEYS) {
         int b = 0;
-        for (int k = 0; k < (int)threadIdx.x; k++) b += W.key_count[k];
+        for (int k = 0; k < (int)threadIdx.x; k++) b += W.ctr->key_count[k];
         base[threadIdx.x] = b;
     }
     __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int key = W.sort_key[i];
-    const unsigned lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(__activemask(), key);
     const int leader = __ffs(peers) - 1;
     int first = 0;
-    if ((int)lane == leader) first = atomicAdd(W.key_count + kShadeKeys + key, __popc(peers));
+    if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
     first = __shfl_sync(peers, first, leader);
-    W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[i];
+    W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[cur][i];
 }
 
-cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
-                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s, uint64_t* launches) {
-    if (n <= 0) return cudaSuccess;
-    WfState Ws = W;
-    if (n >= 4096) {
-        cudaError_t e = cudaMemsetAsync(W.key_count, 0, 2 * kShadeKeys * sizeof(int32_t), s);
-        if (e != cudaSuccess) return e;
-        k_wf_sort_count<<<grid_for(n, 256), 256, 0, s>>>(S, W, n);
-        k_wf_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(W, n);
-        *launches += 2;
-        Ws.active = W.sorted;
+/* end of an iteration: the next active list becomes current */
+__global__ void k_wf_tail(WfState W) {
+    if (threadIdx.x == 0) W.ctr->iter++;
+}
+__global__ void k_wf_tail_loop(WfState W, cudaGraphConditionalHandle loop, uint32_t* status) {
+    if (threadIdx.x == 0) {
+        const int next = (W.ctr->iter & 1) ^ 1;
+        W.ctr->iter++;
+        bool more = W.ctr->n_active[next] > 0;
+        if (more && W.ctr->iter >= WF_ITER_CAP) { atomicOr(status, RT_STATUS_ITER); more = false; }
+        cudaGraphSetConditional(loop, more ? 1u : 0u);
     }
-    k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(S, P, Ws, n, status, stats, counting, regenerate);
-    *launches += 1;
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+/* resident blocks of a grid-stride kernel: every SM filled once */
+template <typename K>
+int resident_blocks(K kernel, int block) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm <= 0)
+        per_sm = 1, sms = sms > 0 ? sms : 1;
+    return sms * per_sm;
+}
+
+}  // namespace
+
+cudaError_t rt_wf_start(const WfState& W, cudaStream_t s) {
+    k_wf_start<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_wf_active_init<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
+    return cudaGetLastError();
+}
+
+cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s) {
+    static const int closest_blocks = resident_blocks(k_wf_trace_closest, 128);
+    static const int shadow_blocks = resident_blocks(k_wf_trace_shadow, 128);
+    k_wf_trace_closest<<<closest_blocks, 128, 0, s>>>(W, status, stats, counting);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_wf_trace_shadow<<<shadow_blocks, 128, 0, s>>>(W, status, stats, counting);
+    return cudaGetLastError();
+}
+
+cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
+                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches) {
+    const int n = n_hint >= 0 ? std::min(n_hint, W.slots) : W.slots;
+    k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
+    if (n > 0) {
+        k_wf_sort_count<<<grid_for(n, 256), 256, 0, s>>>(W);
+        k_wf_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(W);
+        k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
+        *launches += 3;
+    }
+    if (has_loop) k_wf_tail_loop<<<1, 32, 0, s>>>(W, loop, status);
+    else k_wf_tail<<<1, 32, 0, s>>>(W);
+    *launches += 2;
     return cudaGetLastError();
 }

@@ -1,5 +1,14 @@
 /*
  * rt_wavefront.h - device state of the wavefront renderer (rt_wavefront.cu).
+ *
+ * One wavefront run renders a batch of jobs (a job = one scene, its render
+ * parameters and its sample buffer) with one pool of path slots: paths of
+ * different jobs share the ray queues and the trace / shade launches.  A
+ * single render is a batch of one.  Everything a launch needs to know about
+ * the current round (job table, sample counts, queue lengths) lives in device
+ * memory, so the per-bounce launch sequence is the same every time and can
+ * be captured once into a CUDA graph whose while-loop runs until no path is
+ * left.
  */
 #ifndef RT_WAVEFRONT_H
 #define RT_WAVEFRONT_H
@@ -9,25 +18,48 @@
 
 enum { WF_RAY_EXT = 0, WF_RAY_SHADOW = 1, WF_RAY_MIS = 2 };
 
+#define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
+#define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
+#define WF_SHADE_KEYS 16
+#define WF_ITER_CAP (1 << 20)      /* bounce iterations of one round before a run gives up */
+
+/* one render of a batch, for the current round of samples */
+struct WfJob {
+    const RtSceneView* view;       /* the job's scene (device) */
+    RtParams P;                    /* chunk_begin / chunk_len: this round's sample indices */
+    float* samples;                /* per-sample radiance, [k][crop pixel][rgb] */
+    long long first;               /* first batch-wide sample id of this job's round */
+    long long count;               /* P.w * P.h * P.chunk_len */
+};
+
+/* device counters of a run; iteration i reads active[i & 1] and fills active[(i + 1) & 1] */
+struct WfCounters {
+    long long total;               /* samples of the round, all jobs */
+    unsigned long long next_sample;/* next batch-wide sample id to start */
+    int32_t n_jobs;
+    int32_t iter;
+    int32_t n_closest, n_shadow;   /* rays queued for the next trace */
+    int32_t n_active[2];
+    int32_t fetch[2];              /* next closest / shadow queue entry to hand out */
+    int32_t key_count[2 * WF_SHADE_KEYS];   /* per shade key: entries, scatter cursor */
+};
+
 /* structure-of-arrays path state; every array has one entry per path slot
  * except the ray queue (3 entries per slot) */
 struct WfState {
-    /* ray queue: origin + MinT, direction + MaxT, (slot << 2) | kind.
+    /* ray queue: origin + MinT, direction + MaxT, (slot << 10) | (job << 2) | kind.
      * Closest-hit rays (extension, MIS) fill [0, 2 * slots), shadow rays
      * [shadow_base, shadow_base + slots): the two ray kinds never share a warp. */
     float4* q_o; float4* q_d; int32_t* q_meta;
-    int32_t* n_rays_next;
-    int32_t* n_shadow_next;
     int32_t shadow_base;
-    int32_t* fetch;              /* [0] closest, [1] shadow: next queue entry to hand out */
-    /* active slot lists (read by the shade kernel / written for the next one) */
-    int32_t* active; int32_t* active_next;
-    /* the active list regrouped by shade key before shading (see shade_key) */
+    int32_t slots;
+    WfCounters* ctr;
+    const WfJob* jobs;
+    /* active slot lists by iteration parity, and the list regrouped by shade key */
+    int32_t* active[2];
     int32_t* sorted; uint8_t* sort_key;
-    int32_t* key_count;      /* [0, 16) entries per key, [16, 32) scatter cursors */
-    int32_t* n_active; int32_t* n_active_next;
-    unsigned long long* next_sample;
     /* path state */
+    uint8_t* job;            /* job of the slot's path */
     int4* pix;               /* crop x, crop y, sample index in chunk, sample index t */
     uint32_t* rng_n;         /* draws consumed from the path's Philox stream */
     float4* coeff; float4* rad;
@@ -45,14 +77,19 @@ struct WfState {
     float4* ext_hit; int32_t* ext_sub;
     float4* mis_hit; int32_t* mis_sub;
     uint8_t* occluded;
-    float* samples;          /* per-sample radiance, [k][crop pixel][rgb] */
 };
 
-cudaError_t rt_wf_start(const RtSceneView* S, const RtParams& P, const WfState& W, int slots, cudaStream_t s);
-cudaError_t rt_wf_trace(const RtSceneView* S, const WfState& W, int n_closest, int n_shadow, uint32_t* status,
-                        unsigned long long* stats, bool counting, cudaStream_t s);
-/* Shades the n active paths; launches += the kernels it started. */
-cudaError_t rt_wf_shade(const RtSceneView* S, const RtParams& P, const WfState& W, int n, uint32_t* status,
-                        unsigned long long* stats, bool counting, bool regenerate, cudaStream_t s, uint64_t* launches);
+/* Starts the round: every slot takes a camera sample, the first active list
+ * is built.  The counters must hold the round's total / n_jobs and zeros. */
+cudaError_t rt_wf_start(const WfState& W, cudaStream_t s);
+/* Traces the queued closest-hit and shadow rays (lengths read on the device). */
+cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s);
+/* Shades the active paths, then advances the iteration; with `loop` set
+ * (inside a captured while-loop), also sets the loop's condition to "paths
+ * remain".  n_hint: the active count when the host knows it (grids sized to
+ * it), -1 inside a graph (grids cover every slot, surplus blocks return).
+ * Kernel launches are added to *launches. */
+cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
+                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches);
 
 #endif

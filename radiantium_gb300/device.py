@@ -101,6 +101,20 @@ class Device:
         p = settings.to_c()
         self._check(self.lib.rt_render_device(self.h, C.byref(p), C.c_void_p(out_ptr), C.c_void_p(stream or None)))
 
+    def render_batch(self, items) -> list:
+        """Renders [(Device holding the scene, RenderSettings), ...] as one wavefront
+        on this device's context; returns the averaged films (x, y, rgb)."""
+        outs, arr = [], (N.BatchItem * len(items))()
+        for i, (d, st) in enumerate(items):
+            w, h = d._crop(st)
+            out = np.zeros(w * h * 3, dtype=np.float32)
+            outs.append(out.reshape(w, h, 3))
+            arr[i].scene_ctx = d.h
+            arr[i].params = st.to_c()
+            arr[i].out_rgb = out.ctypes.data
+        self._check(self.lib.rt_render_batch(self.h, arr, len(items)))
+        return outs
+
     def render_device_noalloc(self, settings: RenderSettings, out_ptr: int, stream: int = 0):
         """Same film as render_device, rendered out of the library's fixed device
         scratch (RT_NOALLOC_SCRATCH_BYTES) with no device allocation."""

@@ -103,6 +103,10 @@ class RenderParams(C.Structure):
                 ("x0", C.c_int32), ("y0", C.c_int32), ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("scene_ctx", C.c_void_p), ("params", RenderParams), ("out_rgb", C.c_void_p)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64),
                 ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64), ("instance_visits", C.c_uint64),
@@ -134,10 +138,12 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_get_stats", "rt_set_counting",
+    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_render_batch", "rt_get_stats", "rt_set_counting",
     "rt_set_renderer", "rt_cancel",
 ]
-RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT = 0, 1, 2
+RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
+MAX_BATCH = 256
+MAX_SLOTS = 1 << 21       # path slots in flight (wavefront)
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024   # RT_NOALLOC_SCRATCH_BYTES
 
 _lib = None
@@ -173,6 +179,8 @@ def _declare(lib):
     lib.rt_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.rt_set_counting.restype = C.c_int
     lib.rt_set_counting.argtypes = [vp, C.c_int]
+    lib.rt_render_batch.restype = C.c_int
+    lib.rt_render_batch.argtypes = [vp, C.POINTER(BatchItem), C.c_int]
     lib.rt_set_renderer.restype = C.c_int
     lib.rt_set_renderer.argtypes = [vp, C.c_int]
     lib.rt_cancel.restype = C.c_int

@@ -117,7 +117,7 @@ def test_camera_rays_trace(dev, cornell):
     assert_hits_equal(dev.trace_closest(rays), orc.trace_closest(rays))
 
 
-RENDERERS = [N.RENDERER_MEGAKERNEL, N.RENDERER_WAVEFRONT]
+RENDERERS = [N.RENDERER_MEGAKERNEL, N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH]
 
 
 def _render(dev, st, renderer):
@@ -133,7 +133,7 @@ def _render(dev, st, renderer):
 @pytest.mark.parametrize("strategy", [N.STRATEGY_UNIFORM, N.STRATEGY_ALL])
 def test_render_cornell_bitexact(dev, cornell, method, strategy, renderer):
     s, st, orc = cornell
-    if renderer == N.RENDERER_WAVEFRONT and strategy == N.STRATEGY_ALL:
+    if renderer in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) and strategy == N.STRATEGY_ALL:
         pytest.skip("the wavefront renderer runs the Uniform light strategy")
     dev.upload(s)
     st = st.replace(spp=3, method=method, strategy=strategy)
