@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["instanced", "cornell", "volume"], default="instanced")
+    ap.add_argument("--workload", choices=["instanced", "cornell", "volume", "batch"], default="instanced")
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -372,8 +372,239 @@ def run_ours(args):
     return 0
 
 
+BATCH_STEPS_PER_FRAME = 16
+
+
+def batch_step_settings(scenes, step):
+    """Step `step` of the batched workload: every scene renders the next
+    1/16 of its spp (at least 1 sample per pixel)."""
+    out = []
+    for s, st in scenes:
+        spp = max(1, round(st.spp / BATCH_STEPS_PER_FRAME))
+        out.append(st.replace(spp=spp, sample_begin=step * spp))
+    return out
+
+
+def batch_config(scenes, step_settings):
+    tris = [s.triangle_count for s, _ in scenes]
+    return {"workload": f"batch: {len(scenes)} independent scenes (displaced sphere or box, log-uniform "
+                        f"{min(tris)}-{max(tris)} triangles, diffuse / GGX conductor / rough dielectric, quad light "
+                        "or env), path MIS, rendered as one wavefront (rt_render_batch)",
+            "scenes": len(scenes), "triangles": int(sum(tris)),
+            "films": sorted({f"{s.camera.width}x{s.camera.height}" for s, _ in scenes}),
+            "spp_frame_range": [min(st.spp for _, st in scenes), max(st.spp for _, st in scenes)],
+            "max_depth_range": [min(st.max_depth for _, st in scenes), max(st.max_depth for _, st in scenes)],
+            "samples_per_step": int(sum(s.camera.width * s.camera.height * st.spp
+                                        for (s, _), st in zip(scenes, step_settings))),
+            "steps_per_frame": BATCH_STEPS_PER_FRAME}
+
+
+def run_batch_reference(args):
+    """The oracle on a bounded sample of the batch: a centre crop of every 4th scene."""
+    from radiantium_gb300 import procedural
+    from oracle.oracle import OracleScene
+    scenes = procedural.batch_scenes()
+    cores = os.cpu_count() or 1
+    pick = scenes[::4]
+    orcs = [(OracleScene(s), st, s) for s, st in pick]
+    crops = []
+    for orc, st, s in orcs:
+        w, h = min(32, s.camera.width), min(32, s.camera.height)
+        crops.append((orc, st.replace(spp=1, x0=(s.camera.width - w) // 2, y0=(s.camera.height - h) // 2,
+                                      width=w, height=h), w * h))
+    t0 = time.perf_counter()
+    for orc, cal, _ in crops:
+        orc.render(cal, threads=cores)
+    t1 = time.perf_counter() - t0
+    spp = int(max(1, (150.0 / (args.steps + args.warmup)) / max(t1, 1e-3)))
+    def step(i):
+        for orc, cal, _ in crops:
+            orc.render(cal.replace(spp=spp, sample_begin=i * spp), threads=cores)
+    for i in range(args.warmup):
+        step(i)
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        step(args.warmup + i)
+        times.append(time.perf_counter() - t0)
+    samples = sum(n for _, _, n in crops) * spp
+    ms = 1000.0 * float(np.mean(times))
+    value = samples / (ms / 1000.0)
+    desc = f"centre 32x32 crops of {len(crops)} of the {len(scenes)} scenes x {spp} spp per step ({samples} samples/step)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+        "config": dict(batch_config(scenes, batch_step_settings(scenes, 0)), step=desc),
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
+                         "sample": desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
+                                          "(oracle/) runs on all host cores"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    for orc, _, _ in orcs:
+        orc.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """The batched workload: 32 scenes rendered as one wavefront per step."""
+    import torch
+    from radiantium_gb300 import native as N
+    from radiantium_gb300 import procedural
+    from radiantium_gb300.device import Device
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    scenes = procedural.batch_scenes()
+    t0 = time.perf_counter()
+    devs = []
+    for s, _ in scenes:
+        d = Device(local)
+        d.upload(s)
+        devs.append(d)
+    upload_s = time.perf_counter() - t0
+    host = Device(local)
+    mode = N.RENDERER_WAVEFRONT_GRAPH if args.renderer == "graph" else N.RENDERER_WAVEFRONT
+    host.set_renderer(mode)
+    films = [torch.empty(s.camera.width * s.camera.height * 3, dtype=torch.float32, device="cuda")
+             for s, _ in scenes]
+    ptrs = [f.data_ptr() for f in films]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    base = rank * (args.warmup + args.steps + 64)
+
+    def items(step):
+        return list(zip(devs, batch_step_settings(scenes, base + step)))
+
+    samples_step = sum(s.camera.width * s.camera.height * st.spp
+                       for (s, _), st in zip(scenes, batch_step_settings(scenes, 0)))
+    host.set_counting(True)
+    host.render_batch_device(items(0), ptrs, stream)
+    counts = host.stats()
+    host.set_counting(False)
+    for i in range(args.warmup):
+        host.render_batch_device(items(i), ptrs, stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, loop_ms, shade_ms, launches = [], 0.0, 0.0, 0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        host.render_batch_device(items(args.warmup + i), ptrs, stream)
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        st = host.stats()
+        loop_ms += st["render_kernel_ms"]
+        shade_ms += st["shade_kernel_ms"]
+        launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = samples_step * world / (ms_step / 1000.0)
+
+    e2e = None
+    if not args.no_e2e:
+        times = []
+        for i in range(args.steps):
+            t0 = time.perf_counter()
+            host.render_batch(items(args.warmup + args.steps + i))
+            times.append(time.perf_counter() - t0)
+        e2e = {"value": samples_step * world / float(np.mean(times)), "unit": "samples/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": int(sum(s.camera.width * s.camera.height * 12 for s, _ in scenes)),
+               "note": f"rt_render_batch into host films; scenes resident (32 x rt_upload_scene, {upload_s:.1f} s "
+                       "incl. BVH builds)"}
+
+    # the same step scene by scene: plain megakernel, and the one-scene wavefront
+    def sequential(renderer):
+        for d in devs:
+            d.set_renderer(renderer)
+        pt = []
+        for i in range(max(1, args.plain_steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for d, stx, p in zip(devs, batch_step_settings(scenes, base + args.warmup + i), ptrs):
+                d.render_device(stx, p, stream)
+            e1.record()
+            e1.synchronize()
+            pt.append(e0.elapsed_time(e1))
+        for d in devs:
+            d.set_renderer(N.RENDERER_AUTO)
+        return samples_step / (float(np.mean(pt)) / 1000.0)
+
+    plain = seq_wf = None
+    if args.plain_steps > 0:
+        plain = {"value": sequential(N.RENDERER_MEGAKERNEL), "unit": "samples/s", "steps": args.plain_steps,
+                 "note": "plain megakernel, the 32 scenes one after another, same passes, identical films"}
+        seq_wf = {"value": sequential(N.RENDERER_WAVEFRONT), "unit": "samples/s", "steps": args.plain_steps,
+                  "note": "one-scene wavefront (rt_render_device), the 32 scenes one after another"}
+
+    alg_bytes_step = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
+                      + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"] + B_FILM * counts["samples"])
+    graph = mode == N.RENDERER_WAVEFRONT_GRAPH
+    achieved = alg_bytes_step / (loop_ms / args.steps / 1000.0) / 1e9
+    peak, peak_src = measured_peak()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        s0, st0 = scenes[1]
+        cpu = cpu_baseline(s0, st0, args.cpu_seconds)
+        cpu["sample"] = "scene 1 of the batch: " + cpu["sample"]
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+        "config": dict(batch_config(scenes, batch_step_settings(scenes, 0)),
+                       parallelism=f"replicas x{world} (independent sample passes)",
+                       l2="256 MiB flush between timed steps (outside the CUDA events)",
+                       renderer="batched wavefront, bounce loop as a CUDA graph while-loop" if graph
+                       else "batched wavefront, bounce loop driven from the host"),
+        "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src,
+                     "kernel": ("whole bounce loop (graph: trace + sort + shade)" if graph
+                                else "k_wf_trace_closest + k_wf_trace_shadow"),
+                     "kernel_ms_per_step": loop_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
+        "plain_megakernel": plain,
+        "sequential_wavefront": seq_wf,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
+                                                   "prim_tests", "instance_visits", "invalid_samples")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for d in devs:
+        d.close()
+    host.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "batch":
+        return run_batch_reference(args) if args.impl == "reference" else run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

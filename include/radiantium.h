@@ -328,10 +328,15 @@ typedef struct rt_batch_item {
  * batch.  Each film equals what rt_render gives for the same item, bit for
  * bit.  Every item must use the `path` integrator with the Uniform light
  * strategy, and all scene contexts must be on the batch context's device.
- * The bounce loop runs as a CUDA graph unless rt_set_renderer selected
- * RT_RENDERER_WAVEFRONT.  No counterpart in the reference, which renders one
- * scene per process (Radiantium.Cli/Program.cs). */
+ * The bounce loop is driven from the host, or runs as a CUDA graph when
+ * rt_set_renderer selected RT_RENDERER_WAVEFRONT_GRAPH.  No counterpart in
+ * the reference, which renders one scene per process
+ * (Radiantium.Cli/Program.cs). */
 int rt_render_batch(void* ctx, const rt_batch_item* items, int n);
+
+/* Same, every out_rgb a device pointer written on `stream` (NULL = the
+ * context stream); returns once the films are written. */
+int rt_render_batch_device(void* ctx, const rt_batch_item* items, int n, void* stream);
 
 /* Requests cancellation of a running render (Renderer.Stop, BlockBasedRenderer.cs:85-88). */
 int rt_cancel(void* ctx);

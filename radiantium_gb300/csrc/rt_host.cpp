@@ -920,8 +920,9 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH);
 }
 
-/* rt_render_batch: every item's film through one wavefront run */
-void render_batch(Ctx* c, const rt_batch_item* items, int n) {
+/* rt_render_batch(_device): every item's film through one wavefront run;
+ * out_rgb are host pointers, or device pointers written on `user` */
+void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cudaStream_t user) {
     if (!items || n <= 0 || n > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: 1 to 256 items");
     std::vector<WfJobIn> jobs((size_t)n);
     std::vector<int64_t> film_off((size_t)n);
@@ -950,20 +951,24 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n) {
         film_off[i] = film_floats;
         film_floats += (int64_t)P.w * P.h * 3;
     }
-    cudaStream_t s = c->stream;
+    cudaStream_t s = device_out && user ? user : c->stream;
     ensure(&c->film, &c->film_bytes, (size_t)film_floats * 4);
-    ensure(&c->out, &c->out_bytes, (size_t)film_floats * 4);
+    if (!device_out) ensure(&c->out, &c->out_bytes, (size_t)film_floats * 4);
     for (int i = 0; i < n; i++) jobs[i].film = c->film + film_off[i];
     CK(cudaMemsetAsync(c->film, 0, (size_t)film_floats * 4, s));
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
-    wavefront_run(c, jobs, s, c->renderer != RT_RENDERER_WAVEFRONT);
+    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH);
     uint64_t samples = 0;
     for (int i = 0; i < n; i++) {
         const int64_t npix = (int64_t)jobs[i].P.w * jobs[i].P.h;
-        CK(rt_launch_finalize(c->out + film_off[i], c->film + film_off[i], npix, (float)jobs[i].P.spp, s));
-        CK(cudaMemcpyAsync(items[i].out_rgb, c->out + film_off[i], (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
+        if (device_out) {
+            CK(rt_launch_finalize(items[i].out_rgb, c->film + film_off[i], npix, (float)jobs[i].P.spp, s));
+        } else {
+            CK(rt_launch_finalize(c->out + film_off[i], c->film + film_off[i], npix, (float)jobs[i].P.spp, s));
+            CK(cudaMemcpyAsync(items[i].out_rgb, c->out + film_off[i], (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
+        }
         samples += (uint64_t)npix * jobs[i].P.spp;
     }
     CK(cudaStreamSynchronize(s));
@@ -1111,7 +1116,11 @@ int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb
 }
 int rt_render_batch(void* ctx, const rt_batch_item* items, int n) {
     Ctx* c = (Ctx*)ctx;
-    return run(c, [&]() { render_batch(c, items, n); });
+    return run(c, [&]() { render_batch(c, items, n, false, nullptr); });
+}
+int rt_render_batch_device(void* ctx, const rt_batch_item* items, int n, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render_batch(c, items, n, true, (cudaStream_t)stream); });
 }
 int rt_render_device_noalloc(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
     Ctx* c = (Ctx*)ctx;

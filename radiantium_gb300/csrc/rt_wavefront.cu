@@ -511,13 +511,29 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
     }
 }
 
-/* the active paths of this iteration, one thread each over the sorted list;
- * the grid covers every slot and the blocks past the active count return */
-__global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting) {
+/* the active paths of this iteration, one thread each over the sorted list:
+ * either a grid sized to the active count, or (`dynamic`, inside a graph
+ * where the count is unknown at launch) a resident grid whose warps take the
+ * next 32 entries from a counter until the list is done */
+__global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting,
+                                                       bool dynamic) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+    if (!dynamic) {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&W.ctr->shade_fetch, 32);
+        base = __shfl_sync(kFullWarp, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+        __syncwarp();
+    }
 }
 
 __global__ void k_wf_active_init(WfState W) {
@@ -546,21 +562,25 @@ DF int shade_key(const WfState& W, int slot) {
 __global__ void k_wf_phase(WfState W) {
     if (threadIdx.x == 0) {
         WfCounters* c = W.ctr;
-        c->n_closest = 0; c->n_shadow = 0; c->fetch[0] = 0; c->fetch[1] = 0;
+        c->n_closest = 0; c->n_shadow = 0; c->fetch[0] = 0; c->fetch[1] = 0; c->shade_fetch = 0;
         c->n_active[(c->iter & 1) ^ 1] = 0;
     }
     if (threadIdx.x < 2 * WF_SHADE_KEYS) W.ctr->key_count[threadIdx.x] = 0;
 }
 
+/* both sort kernels are grid-stride loops: one pass with a grid sized to the
+ * active count, several with a resident grid inside a graph */
 __global__ void __launch_bounds__(256) k_wf_sort_count(WfState W) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int key = shade_key(W, W.active[cur][i]);
-    W.sort_key[i] = (uint8_t)key;
-    const unsigned peers = __match_any_sync(__activemask(), key);
-    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.ctr->key_count + key, __popc(peers));
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        if (i >= n) break;
+        const int key = shade_key(W, W.active[cur][i]);
+        W.sort_key[i] = (uint8_t)key;
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.ctr->key_count + key, __popc(peers));
+    }
 }
 
 /* counting-sort scatter: entries of one key stay together, in any order
@@ -577,15 +597,17 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
     }
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int key = W.sort_key[i];
-    const unsigned peers = __match_any_sync(__activemask(), key);
-    const int leader = __ffs(peers) - 1;
-    int first = 0;
-    if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
-    first = __shfl_sync(peers, first, leader);
-    W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[cur][i];
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        if (i >= n) break;
+        const int key = W.sort_key[i];
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int leader = __ffs(peers) - 1;
+        int first = 0;
+        if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
+        first = __shfl_sync(peers, first, leader);
+        W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[cur][i];
+    }
 }
 
 /* end of an iteration: the next active list becomes current */
@@ -636,12 +658,16 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
 
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
                         cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches) {
-    const int n = n_hint >= 0 ? std::min(n_hint, W.slots) : W.slots;
+    static const int sort_blocks = resident_blocks(k_wf_sort_scatter, 256);
+    static const int shade_blocks = resident_blocks(k_wf_shade, 128);
+    const bool known = n_hint >= 0;
+    const int n = known ? std::min(n_hint, W.slots) : W.slots;
     k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
     if (n > 0) {
-        k_wf_sort_count<<<grid_for(n, 256), 256, 0, s>>>(W);
-        k_wf_sort_scatter<<<grid_for(n, 256), 256, 0, s>>>(W);
-        k_wf_shade<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
+        const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
+        k_wf_sort_count<<<sb, 256, 0, s>>>(W);
+        k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
+        k_wf_shade<<<known ? grid_for(n, 128) : (unsigned)shade_blocks, 128, 0, s>>>(W, status, stats, counting, !known);
         *launches += 3;
     }
     if (has_loop) k_wf_tail_loop<<<1, 32, 0, s>>>(W, loop, status);

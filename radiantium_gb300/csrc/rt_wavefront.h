@@ -41,6 +41,8 @@ struct WfCounters {
     int32_t n_closest, n_shadow;   /* rays queued for the next trace */
     int32_t n_active[2];
     int32_t fetch[2];              /* next closest / shadow queue entry to hand out */
+    int32_t shade_fetch;           /* next sorted entry to shade (resident-grid shading) */
+    int32_t pad;
     int32_t key_count[2 * WF_SHADE_KEYS];   /* per shade key: entries, scatter cursor */
 };
 

@@ -115,6 +115,15 @@ class Device:
         self._check(self.lib.rt_render_batch(self.h, arr, len(items)))
         return outs
 
+    def render_batch_device(self, items, out_ptrs, stream: int = 0):
+        """Same as render_batch with each film written to device memory out_ptrs[i] on `stream`."""
+        arr = (N.BatchItem * len(items))()
+        for i, ((d, st), ptr) in enumerate(zip(items, out_ptrs)):
+            arr[i].scene_ctx = d.h
+            arr[i].params = st.to_c()
+            arr[i].out_rgb = ptr
+        self._check(self.lib.rt_render_batch_device(self.h, arr, len(items), C.c_void_p(stream or None)))
+
     def render_device_noalloc(self, settings: RenderSettings, out_ptr: int, stream: int = 0):
         """Same film as render_device, rendered out of the library's fixed device
         scratch (RT_NOALLOC_SCRATCH_BYTES) with no device allocation."""

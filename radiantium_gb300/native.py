@@ -138,7 +138,7 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_render_batch", "rt_get_stats", "rt_set_counting",
+    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_get_stats", "rt_set_counting",
     "rt_set_renderer", "rt_cancel",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
@@ -181,6 +181,8 @@ def _declare(lib):
     lib.rt_set_counting.argtypes = [vp, C.c_int]
     lib.rt_render_batch.restype = C.c_int
     lib.rt_render_batch.argtypes = [vp, C.POINTER(BatchItem), C.c_int]
+    lib.rt_render_batch_device.restype = C.c_int
+    lib.rt_render_batch_device.argtypes = [vp, C.POINTER(BatchItem), C.c_int, vp]
     lib.rt_set_renderer.restype = C.c_int
     lib.rt_set_renderer.argtypes = [vp, C.c_int]
     lib.rt_cancel.restype = C.c_int

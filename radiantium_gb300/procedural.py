@@ -231,6 +231,68 @@ def volume_sphere(width=512, height=512, sphere_n=204, seed=11):
     return s, settings
 
 
+def displaced_box(n: int, seed: int, amplitude: float = 0.05, frequency: float = 2.5) -> Mesh:
+    """Unit cube with n x n quads per face (12 n^2 triangles), each vertex pushed out
+    along its ray from the centre by 1 + amplitude * noise."""
+    sph = displaced_sphere(n, seed, amplitude=0.0)
+    d = sph.positions.astype(np.float64)
+    cube = d / np.abs(d).max(1, keepdims=True)
+    r = 1.0 + amplitude * value_noise(cube * frequency, seed + 1)
+    return Mesh((cube * r[:, None]).astype(np.float32), sph.indices)
+
+
+def batch_scene(i: int, seed: int = 11):
+    """Scene i of the batched workload: one displaced sphere or box with a
+    log-uniform triangle count in [10k, 2M] and a diffuse / GGX conductor /
+    rough dielectric material on a diffuse ground, lit by a quad light or a
+    Gaussian-lobe environment; resolution in {128 ... 1024}, spp in [16, 256],
+    max depth in [4, 16]."""
+    rng = np.random.default_rng(seed * 1000 + i)
+    tris = math.exp(rng.uniform(math.log(1e4), math.log(2e6)))
+    n = max(2, int(round(math.sqrt(tris / 12.0))))
+    res = [128, 256, 384, 512, 768, 1024]
+    w = int(rng.choice(res))
+    h = int(rng.choice([r for r in res if r <= w] or [w]))
+    spp = int(round(math.exp(rng.uniform(math.log(16), math.log(256)))))
+    depth = int(rng.integers(4, 17))
+    s = SceneDesc(camera=Camera.look_at(w, h, 40.0, (0.0, 1.8, 4.2), (0.0, 0.9, 0.0)), name=f"batch{i}")
+    zero = s.add_const(0.0)
+    one = s.add_const(1.0)
+    kind = int(rng.integers(0, 3))
+    if kind == 0:
+        albedo = tuple(float(x) for x in rng.uniform(0.2, 0.8, 3))
+        mat = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const(albedo)))
+    elif kind == 1:
+        rough = s.add_const(math.sqrt(float(rng.uniform(0.05, 0.5))))
+        mat = s.add_material(Material(N.MAT_ROUGH_METAL, N.DIST_GGX, tex_roughness=rough, tex_anisotropic=zero,
+                                      eta=CU_ETA, k=CU_K))
+    else:
+        rough = s.add_const(math.sqrt(float(rng.uniform(0.05, 0.5))))
+        mat = s.add_material(Material(N.MAT_ROUGH_GLASS, N.DIST_GGX, tex_r=one, tex_t=one, tex_roughness=rough,
+                                      tex_anisotropic=zero, eta_a=1.0, eta_b=1.5))
+    shape = displaced_sphere(n, seed + i) if rng.uniform() < 0.5 else displaced_box(n, seed + i)
+    shape = shape.transformed(Mat4.scale((0.8, 0.8, 0.8)) * Mat4.translation((0.0, 0.9, 0.0)))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(shape), material=mat))
+    ground = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.5, 0.5, 0.5))))
+    s.groups.append(Group(N.GROUP_MESH, s.add_mesh(quad((-10, 0, -10), (-10, 0, 10), (10, 0, 10), (10, 0, -10))),
+                          material=ground))
+    if rng.uniform() < 0.5:
+        lm = s.add_material(Material(N.MAT_DIFFUSE, tex_r=s.add_const((0.5, 0.5, 0.5))))
+        light = quad((-0.6, 3.5, -0.6), (0.6, 3.5, -0.6), (0.6, 3.5, 0.6), (-0.6, 3.5, 0.6))
+        s.groups.append(Group(N.GROUP_MESH, s.add_mesh(light), material=lm, emissive=True, le=(25.0, 25.0, 25.0)))
+    else:
+        env = s.add_texture(gaussian_lobe_env(128, 64, seed + i))
+        s.groups.append(Group(N.GROUP_INFINITE_LIGHT, env))
+    settings = RenderSettings(N.INTEGRATOR_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=depth, min_depth=3,
+                              rr_threshold=0.99, spp=spp, seed=1 + i)
+    return s, settings
+
+
+def batch_scenes(count: int = 32, seed: int = 11):
+    """The batched workload: `count` independent scenes (batch_scene)."""
+    return [batch_scene(i, seed) for i in range(count)]
+
+
 WORKLOADS = {
     "cornell": cornell_box,
     "instanced": instanced_spheres,

@@ -88,6 +88,7 @@ def test_batch_repeats_and_single_graph_render(scenes):
     want = _singles(items)
     host = Device(0)
     try:
+        host.set_renderer(N.RENDERER_WAVEFRONT_GRAPH)
         for _ in range(2):
             got = host.render_batch(items)
             for g, w in zip(got, want):
