@@ -293,6 +293,39 @@ int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb
  * The film is the same as rt_render_device's, bit for bit. */
 int rt_render_device_noalloc(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream);
 
+/* ---- gradients (no counterpart in the reference) ----------------------------
+ * The reference renders only; these entry points differentiate its `path`
+ * integrator with MIS (PathTracer.Mis, Integrators/PathTracer.cs:192-270) with
+ * respect to material parameters, for inverse rendering on top of the same
+ * scenes.  The parameters are the texels of one albedo texture (the `r`
+ * texture of diffuse and rough_plastic materials) and the GGX / Beckmann
+ * alpha = roughness^2 of chosen rough_plastic / rough_metal materials. */
+#define RT_ADJ_MAX_ALPHA 1024
+typedef struct rt_adjoint_desc {
+    int32_t albedo_texture;          /* texture index, or -1 for no albedo parameters */
+    int32_t alpha_count;             /* 0 .. RT_ADJ_MAX_ALPHA */
+    const int32_t* alpha_materials;  /* material indices whose alpha is a parameter */
+} rt_adjoint_desc;
+
+/* The film the gradients refer to (same as rt_render). */
+int rt_adjoint_forward(void* ctx, const rt_render_params* params, float* out_rgb);
+
+/* Gradient of sum over the crop of dL_dimage * I with respect to the
+ * parameters, I the film of `params` (crop layout like rt_render's output):
+ * path replay with detached sampling, the same random numbers as the
+ * forward film.  grad_albedo: the albedo texture's width * height * 3 floats
+ * in its ColorBuffer layout; grad_alpha: alpha_count floats, d/d alpha in the
+ * order of alpha_materials.  Gradients are float sums of atomic adds, so the
+ * last bits vary between runs. */
+int rt_adjoint_backward(void* ctx, const rt_render_params* params, const rt_adjoint_desc* desc,
+                        const float* dL_dimage, float* grad_albedo, float* grad_alpha);
+
+/* Replaces the texels (width * height * 3 floats, ColorBuffer layout) of one
+ * texture of the uploaded scene without rebuilding anything else: an albedo
+ * map, or the 1x1 roughness texture that sets a material's alpha.  Textures
+ * of infinite lights are rejected (their sampling tables would go stale). */
+int rt_update_texture(void* ctx, int texture, const float* texels);
+
 /* Counters of the last render / trace call (Stopwatch/Logger counterpart). */
 int rt_get_stats(void* ctx, rt_stats* out);
 

@@ -60,6 +60,14 @@ struct Ctx {
     RtSceneView* d_view = nullptr;             /* device copy of `view` handed to the kernels */
     bool has_scene = false;
     int width = 0, height = 0;
+    std::vector<RtTexture> h_textures;         /* host copies for the adjoint / texture updates */
+    std::vector<RtMaterial> h_materials;
+    std::vector<uint8_t> env_texture;          /* texture feeds an infinite light's sampling table */
+    /* adjoint scratch */
+    float* adj_dldi = nullptr; size_t adj_dldi_bytes = 0;
+    float* adj_galb = nullptr; size_t adj_galb_bytes = 0;
+    float* adj_galpha = nullptr; size_t adj_galpha_bytes = 0;
+    int* adj_slot = nullptr; size_t adj_slot_bytes = 0;
     /* render scratch */
     float* samples = nullptr; size_t samples_bytes = 0;
     float* film = nullptr; size_t film_bytes = 0;
@@ -164,6 +172,7 @@ void ensure_wf(Ctx* c, int slots) {
     W.ext_hit = wf_alloc<float4>(c, n); W.ext_sub = wf_alloc<int32_t>(c, n);
     W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
     W.occluded = wf_alloc<uint8_t>(c, n);
+    W.adj_rho = wf_alloc<float4>(c, n);
     if (!c->d_ctr) CK(cudaMalloc((void**)&c->d_ctr, sizeof(WfCounters)));
     if (!c->h_ctr) CK(cudaMallocHost((void**)&c->h_ctr, sizeof(WfCounters)));
     if (!c->d_jobs) CK(cudaMalloc((void**)&c->d_jobs, WF_MAX_JOBS * sizeof(WfJob)));
@@ -591,6 +600,10 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.instances = upload(c, insts);
     v.materials = upload(c, mats);
     v.textures = upload(c, texs);
+    c->h_textures = texs;
+    c->h_materials = mats;
+    c->env_texture.assign(texs.size(), 0);
+    for (int li : infinite) c->env_texture[lights[li].ref] = 1;
     v.texels = upload(c, texels);
     v.media = upload(c, meds);
     v.lights = upload(c, lights);
@@ -815,7 +828,8 @@ void ensure_wf_graph(Ctx* c, const WfState& W) {
  * paths share the path slots, queues and launches (rt_wavefront.cu).  The
  * bounce loop is driven from the host (per-phase timing) or, with
  * `use_graph`, runs as one CUDA graph launch per round. */
-void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, bool use_graph) {
+void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, bool use_graph,
+                   const WfAdjoint* adj = nullptr) {
     if (jobs.empty() || jobs.size() > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "wavefront: 1 to 256 jobs per run");
     std::vector<int> done(jobs.size(), 0);
     ensure_events(c, 4);
@@ -853,30 +867,33 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             d.count = (int64_t)J.P.w * J.P.h * clen[k];
             first += d.count;
         }
-        std::memset(c->h_ctr, 0, sizeof(WfCounters));
-        c->h_ctr->total = total;
-        c->h_ctr->n_jobs = (int)act.size();
         CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, act.size() * sizeof(WfJob), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
         WfState W = c->wf;
         W.slots = slots;
         W.shadow_base = 2 * slots;
-        CK(rt_wf_start(W, s));
-        launches += 2;
-        if (use_graph) {
-            ensure_wf_graph(c, W);
-            CK(cudaEventRecord(c->events[0], s));
-            CK(cudaGraphLaunch(c->wf_exec, s));
-            CK(cudaEventRecord(c->events[1], s));
-            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
-            launches += 7 * iters;
-            trace_launches += 2 * iters;
-            float t = 0;
-            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
-            trace_ms += t;                      /* the whole loop: not split by phase */
-        } else {
+        /* one pass over the round's samples: start every slot, bounce until no path is left */
+        auto run_pass = [&](int pass) {
+            std::memset(c->h_ctr, 0, sizeof(WfCounters));
+            c->h_ctr->total = total;
+            c->h_ctr->n_jobs = (int)act.size();
+            CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+            CK(rt_wf_start(W, s));
+            launches += 2;
+            if (use_graph && pass == WF_PASS_RENDER) {
+                ensure_wf_graph(c, W);
+                CK(cudaEventRecord(c->events[0], s));
+                CK(cudaGraphLaunch(c->wf_exec, s));
+                CK(cudaEventRecord(c->events[1], s));
+                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
+                launches += 7 * iters;
+                trace_launches += 2 * iters;
+                float t = 0;
+                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
+                trace_ms += t;                  /* the whole loop: not split by phase */
+                return;
+            }
             CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0) {
@@ -887,7 +904,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaEventRecord(c->events[2], s));
                 CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
-                               s, &launches));
+                               s, &launches, pass, adj));
                 CK(cudaEventRecord(c->events[3], s));
                 launches += 2;
                 trace_launches += 2;
@@ -897,7 +914,14 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                 CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
                 CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
             }
+        };
+        if (adj) {
+            run_pass(WF_PASS_FORWARD_RAW);
+            run_pass(WF_PASS_REPLAY);
+            for (size_t k = 0; k < act.size(); k++) done[act[k]] += clen[k];
+            continue;
         }
+        run_pass(WF_PASS_RENDER);
         for (size_t k = 0; k < act.size(); k++) {
             const WfJobIn& J = jobs[act[k]];
             CK(rt_launch_accumulate(J.film, c->h_jobs[k].samples, (int64_t)J.P.w * J.P.h, clen[k], s));
@@ -984,6 +1008,107 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
     c->last.kernel_launches = launches + (uint64_t)n;
 }
 
+/* rt_adjoint_backward: gradients of sum(dL/dI * I) through the MIS path tracer
+ * (rt_adjoint.cu), chunked over samples like the megakernel render */
+void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* d, const float* dldi, float* g_albedo,
+                      float* g_alpha) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (!p || !d || !dldi || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: null params / descriptor / dL_dimage or spp <= 0");
+    if (p->integrator != RT_INTEGRATOR_PATH || p->method != RT_METHOD_MIS)
+        throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: the path integrator with MIS is differentiated");
+    const int ntex = (int)c->h_textures.size(), nmat = (int)c->h_materials.size();
+    if (d->albedo_texture < -1 || d->albedo_texture >= ntex) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: bad albedo texture");
+    if (d->albedo_texture >= 0 && !g_albedo) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: grad_albedo is null");
+    if (d->alpha_count < 0 || d->alpha_count > RT_ADJ_MAX_ALPHA || (d->alpha_count > 0 && (!d->alpha_materials || !g_alpha)))
+        throw RtFail(RT_ERR_INVALID_ARG, "adjoint: bad alpha parameter list");
+    std::vector<int> slot((size_t)std::max(1, nmat), -1);
+    for (int i = 0; i < d->alpha_count; i++) {
+        const int m = d->alpha_materials[i];
+        if (m < 0 || m >= nmat) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: alpha material index out of range");
+        if (slot[m] >= 0) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: alpha material listed twice");
+        const int t = c->h_materials[m].type;
+        if (t != RT_MAT_ROUGH_PLASTIC && t != RT_MAT_ROUGH_METAL)
+            throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: alpha gradients are for rough_plastic and rough_metal");
+        slot[m] = i;
+    }
+    RtParams P{};
+    P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
+    P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;
+    P.seed = p->seed; P.x0 = p->x0; P.y0 = p->y0;
+    P.w = p->width > 0 ? p->width : c->width - p->x0;
+    P.h = p->height > 0 ? p->height : c->height - p->y0;
+    if (P.x0 < 0 || P.y0 < 0 || P.w <= 0 || P.h <= 0 || P.x0 + P.w > c->width || P.y0 + P.h > c->height)
+        throw RtFail(RT_ERR_INVALID_ARG, "adjoint: crop outside the film");
+    P.spp = p->spp; P.sample_begin = p->sample_begin;
+    cudaStream_t s = c->stream;
+    const int64_t npix = (int64_t)P.w * P.h;
+    const int64_t texels = d->albedo_texture >= 0
+        ? (int64_t)c->h_textures[d->albedo_texture].width * c->h_textures[d->albedo_texture].height : 0;
+    ensure(&c->adj_dldi, &c->adj_dldi_bytes, (size_t)npix * 12);
+    ensure(&c->adj_galb, &c->adj_galb_bytes, (size_t)std::max<int64_t>(1, texels) * 12);
+    ensure(&c->adj_galpha, &c->adj_galpha_bytes, (size_t)std::max(1, d->alpha_count) * 4);
+    ensure(&c->adj_slot, &c->adj_slot_bytes, slot.size() * 4);
+    CK(cudaMemcpyAsync(c->adj_dldi, dldi, (size_t)npix * 12, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->adj_slot, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(rt_launch_scale(c->adj_dldi, npix * 3, 1.0f / (float)P.spp, s));
+    CK(cudaMemsetAsync(c->adj_galb, 0, (size_t)std::max<int64_t>(1, texels) * 12, s));
+    CK(cudaMemsetAsync(c->adj_galpha, 0, (size_t)std::max(1, d->alpha_count) * 4, s));
+    CK(cudaMemsetAsync(c->status, 0, 4, s));
+    c->cancel.store(0);
+    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(P.spp, c->sample_budget / std::max<int64_t>(1, npix)));
+    ensure_events(c, 4);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, s));
+    uint64_t launches = 2;
+    if (P.strategy == RT_STRATEGY_UNIFORM) {
+        /* the wavefront: a forward pass keeping each sample's radiance, then the replay */
+        WfAdjoint A{d->albedo_texture, d->alpha_count, c->adj_slot, c->adj_galb, c->adj_galpha, c->adj_dldi};
+        std::vector<WfJobIn> jobs(1);
+        jobs[0].view = c->d_view;
+        jobs[0].P = P;
+        jobs[0].film = nullptr;
+        CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
+        wavefront_run(c, jobs, s, false, &A);
+        launches += c->last.kernel_launches;
+    } else {
+        for (int b = 0; b < P.spp; b += chunk) {
+            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "adjoint cancelled");
+            P.chunk_begin = b;
+            P.chunk_len = std::min(chunk, P.spp - b);
+            CK(rt_launch_adjoint(c->d_view, P, d->albedo_texture, c->adj_slot, c->adj_galb, c->adj_galpha, d->alpha_count,
+                                 c->adj_dldi, c->status, s));
+            launches++;
+        }
+    }
+    CK(cudaEventRecord(e1, s));
+    if (texels > 0) CK(cudaMemcpyAsync(g_albedo, c->adj_galb, (size_t)texels * 12, cudaMemcpyDeviceToHost, s));
+    if (d->alpha_count > 0) CK(cudaMemcpyAsync(g_alpha, c->adj_galpha, (size_t)d->alpha_count * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    check_status(c);
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::memset(&c->last, 0, sizeof(c->last));
+    c->last.samples = (uint64_t)npix * P.spp;
+    c->last.render_kernel_ms = ms;
+    c->last.kernel_launches = launches;
+    c->last.render_launches = launches - 1;
+}
+
+/* rt_update_texture: new texels for one texture of the uploaded scene */
+void update_texture(Ctx* c, int tex, const float* texels) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (tex < 0 || tex >= (int)c->h_textures.size() || !texels) throw RtFail(RT_ERR_INVALID_ARG, "update_texture: bad texture or data");
+    if (c->env_texture[tex]) throw RtFail(RT_ERR_UNSUPPORTED, "update_texture: the texture feeds an infinite light's sampling table; upload the scene again");
+    const RtTexture& t = c->h_textures[tex];
+    CK(cudaMemcpyAsync((void*)(c->view.texels + t.offset), texels, (size_t)t.width * t.height * 12, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+}
+
 void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
     if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
     if (n < 0 || (n > 0 && (!rays || (!hits && !occ)))) throw RtFail(RT_ERR_INVALID_ARG, "trace: bad arguments");
@@ -1064,6 +1189,10 @@ void rt_destroy(void* ctx) {
     free_scene(c);
     if (c->samples) cudaFree(c->samples);
     if (c->film) cudaFree(c->film);
+    if (c->adj_dldi) cudaFree(c->adj_dldi);
+    if (c->adj_galb) cudaFree(c->adj_galb);
+    if (c->adj_galpha) cudaFree(c->adj_galpha);
+    if (c->adj_slot) cudaFree(c->adj_slot);
     if (c->out) cudaFree(c->out);
     if (c->io) cudaFree(c->io);
     if (c->status) cudaFree(c->status);
@@ -1113,6 +1242,19 @@ int rt_render(void* ctx, const rt_render_params* params, float* out_rgb) {
 int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render(c, params, d_out_rgb, false, (cudaStream_t)stream); });
+}
+int rt_adjoint_forward(void* ctx, const rt_render_params* params, float* out_rgb) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render(c, params, out_rgb, true, nullptr); });
+}
+int rt_adjoint_backward(void* ctx, const rt_render_params* params, const rt_adjoint_desc* desc, const float* dL_dimage,
+                        float* grad_albedo, float* grad_alpha) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { adjoint_backward(c, params, desc, dL_dimage, grad_albedo, grad_alpha); });
+}
+int rt_update_texture(void* ctx, int texture, const float* texels) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { update_texture(c, texture, texels); });
 }
 int rt_render_batch(void* ctx, const rt_batch_item* items, int n) {
     Ctx* c = (Ctx*)ctx;

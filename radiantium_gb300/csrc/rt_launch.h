@@ -19,6 +19,11 @@ cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n,
  * `device`, which must be the current device; looked up once per device and
  * process (rt_noalloc.cu) */
 cudaError_t rt_noalloc_scratch(int device, void** ptr);
+/* adjoint (rt_adjoint.cu): gradients into grad_albedo / grad_alpha (accumulated) */
+cudaError_t rt_launch_adjoint(const RtSceneView* S, const RtParams& P, int albedo_tex, const int* alpha_slot,
+                              float* grad_albedo, float* grad_alpha, int n_alpha, const float* dLdI, uint32_t* status,
+                              cudaStream_t stream);
+cudaError_t rt_launch_scale(float* v, int64_t n, float s, cudaStream_t stream);
 cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream);
 
 #endif

@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include "rt_integrators.cuh"
+#include "rt_adjoint.cuh"
 #include "rt_wavefront.h"
 
 using namespace rtd;
@@ -297,9 +298,10 @@ DF bool load_hit(const RtSceneView* S, const Ray& ray, float4 h, int sub, Isect*
     return true;
 }
 
-DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned long long* stats) {
+DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned long long* stats, int pass) {
+    if (pass == WF_PASS_REPLAY) return;
     bool invalid = !IsValid(rad);
-    if (invalid) { rad = c3s(0.0f); atomicAdd(stats + 6, 1ull); }
+    if (invalid && pass == WF_PASS_RENDER) { rad = c3s(0.0f); atomicAdd(stats + 6, 1ull); }
     int4 px = W.pix[slot];
     const RtParams& P = J.P;
     const int64_t npix = (int64_t)P.w * P.h;
@@ -309,13 +311,26 @@ DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned
 
 /* one bounce of PathTracer.Mis / NextEventEstimation / OnlySampleBxdf after the
  * extension hit is known (PathTracer.cs:43-270) */
-DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting) {
+template <bool kAdj>
+DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting,
+                   int pass, const WfAdjoint& A, float* s_alpha) {
     const WfJob& J = W.jobs[W.job[slot]];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;                  /* registers: the path-state stores below cannot alias it */
     uint32_t fl = W.flags[slot];
     float4 cf = W.coeff[slot], rd = W.rad[slot];
     C3 coeff = c3(cf.x, cf.y, cf.z), radiance = c3(rd.x, rd.y, rd.z);
+    /* replay: the sample's radiance from the forward pass and its pixel's dL/dI */
+    C3 Ltot = c3s(0.0f), dL = c3s(0.0f);
+    bool grad = false;
+    if (kAdj) {
+        const int4 q = W.pix[slot];
+        const int64_t pix = (int64_t)q.x * P.h + q.y;
+        const float* ls = J.samples + ((int64_t)q.z * P.w * P.h + pix) * 3;
+        Ltot = c3(ls[0], ls[1], ls[2]);
+        dL = c3(A.dLdI[pix * 3], A.dLdI[pix * 3 + 1], A.dLdI[pix * 3 + 2]);
+        grad = IsValid(Ltot) && (dL.r != 0.0f || dL.g != 0.0f || dL.b != 0.0f);
+    }
 
     /* 1. the direct term scheduled by the previous bounce */
     if (fl & F_PENDING) {
@@ -324,11 +339,13 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
         float lightPdf = pc.w;
         if (P.method == RT_METHOD_MIS) {
             C3 direct = c3s(0);
+            C3 tl = c3s(0.0f), tb = c3s(0.0f);
             if (!(fl & F_DZERO)) {
                 C3 le = c3s(0.0f);
                 if ((fl & F_L1) && !W.occluded[slot]) {
                     float4 l1 = W.pd_l1[slot];
-                    le = le + c3(l1.x, l1.y, l1.z);
+                    tl = c3(l1.x, l1.y, l1.z);
+                    le = le + tl;
                 }
                 if (fl & F_L2) {
                     float4 fr2 = W.pd_fr[slot];
@@ -344,11 +361,23 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
                     } else {
                         li = EvalAllInfinite(S, mr.D);
                     }
-                    if (!IsBlack(li)) le = le + c3(fr2.x, fr2.y, fr2.z) * li * fr2.w / mi.x;
+                    if (!IsBlack(li)) { tb = c3(fr2.x, fr2.y, fr2.z) * li * fr2.w / mi.x; le = le + tb; }
                 }
                 direct = direct + le / lightPdf;
             }
             radiance = radiance + coeffb * direct;
+            if (kAdj && grad) {
+                /* alpha terms of the pending vertex: its two direct terms, then its
+                 * continuation, which carries everything after its direct light */
+                const float4 ar = W.adj_rho[slot];
+                const int aslot = __float_as_int(ar.w);
+                if (aslot >= 0) {
+                    float g = ar.z * Dot3(dL, Ltot - radiance);
+                    if (!IsBlack(tl)) g += ar.x * Dot3(dL, coeffb * tl) / lightPdf;
+                    if (!IsBlack(tb)) g += ar.y * Dot3(dL, coeffb * tb) / lightPdf;
+                    if (g != 0.0f) atomicAdd(s_alpha + aslot, g);
+                }
+            }
         } else { /* NEE */
             C3 e = c3s(0);
             if (!(fl & F_DZERO) && !W.occluded[slot]) { float4 l1 = W.pd_l1[slot]; e = c3(l1.x, l1.y, l1.z); }
@@ -390,6 +419,17 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
                 if (!HasSurface(S, it)) { nray = mkray(it.P, ray.D, ray.MinT); ext = true; break; }
                 /* direct lighting: everything but the two ray casts */
                 const int mat = PrimOf(S, it).material;
+                float4 rho = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                if (kAdj && grad) {
+                    if (UsesAlbedo(S, A.albedo_tex, mat)) {
+                        const C3 R = TexSample(S, A.albedo_tex, it.UV);
+                        const C3 rest = Ltot - radiance;
+                        ScatterAlbedo(S, A.albedo_tex, A.grad_albedo, it.UV,
+                                      c3(R.r > 0 ? dL.r * rest.r / R.r : 0.0f, R.g > 0 ? dL.g * rest.g / R.g : 0.0f,
+                                         R.b > 0 ? dL.b * rest.b / R.b : 0.0f));
+                    }
+                    if (A.alpha_slot) rho.w = __int_as_float(A.alpha_slot[mat]);
+                }
                 int light;
                 float lightPdf = SampleLight(S, rand, &light);
                 if (P.method == RT_METHOD_MIS) {
@@ -408,6 +448,8 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
                                 if (!(dis < 0.001f)) {
                                     fr = fr * AbsCosTheta(Lo(it, ls.Wi));
                                     float weight = PowerHeuristic(ls.Pdf, scatteringPdf);
+                                    if (kAdj && __float_as_int(rho.w) >= 0)
+                                        rho.x = DirectDln(S, mat, Lo(it, wod), Lo(it, ls.Wi), weight, true, it.UV);
                                     C3 l1 = fr * ls.Li * weight / ls.Pdf;
                                     W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
                                     fl |= F_L1;
@@ -429,6 +471,9 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
                                 else weight = PowerHeuristic(scatteringPdf, bxdfToLightPdf);
                             }
                             if (go) {
+                                if (kAdj && __float_as_int(rho.w) >= 0)
+                                    rho.y = DirectDln(S, mat, Lo(it, wod), sample.Wi, sampledSpecular ? 2.0f : weight, false,
+                                                      it.UV);
                                 Ray toLight = Spawn(it, Wo(it, sample.Wi));
                                 V3 wle = Wo(it, -sample.Wi);
                                 W.pd_fr[slot] = make_float4(fr.r, fr.g, fr.b, weight);
@@ -465,9 +510,18 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
                         if (zero) fl |= F_DZERO;
                     }
                 }
+                if (kAdj) W.adj_rho[slot] = rho;
             }
             /* continuation */
             BSample s = MatSample(S, PrimOf(S, it).material, Lo(it, wo), it.UV, rand);
+            if (kAdj && P.method == RT_METHOD_MIS && (fl & F_PENDING)) {
+                float4 rho = W.adj_rho[slot];
+                float rc = 0.0f, rcp;
+                if (__float_as_int(rho.w) >= 0 && s.Pdf > 0.0f)
+                    DlnAlpha(S, PrimOf(S, it).material, Lo(it, wo), s.Wi, it.UV, &rc, &rcp);
+                rho.z = rc;
+                W.adj_rho[slot] = rho;
+            }
             if (P.method != RT_METHOD_BXDF) isSpecularPath = (s.Type & BX_SPECULAR) != 0;
             if (s.Pdf > 0.0f) coeff = coeff * (s.Fr * AbsCosTheta(s.Wi) / s.Pdf);
             else { done = true; break; }
@@ -500,7 +554,7 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
         W.active[next][a] = slot;
         return;
     }
-    finish_path(J, W, slot, radiance, stats);
+    finish_path(J, W, slot, radiance, stats, pass);
     if (counting) warp_add64(stats + 0, 1u);
     if (start_path(W, slot, true)) {
         int a = warp_append(&W.ctr->n_active[next], true);
@@ -512,27 +566,39 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
 }
 
 /* the active paths of this iteration, one thread each over the sorted list:
- * either a grid sized to the active count, or (`dynamic`, inside a graph
- * where the count is unknown at launch) a resident grid whose warps take the
- * next 32 entries from a counter until the list is done */
+ * either a grid sized to the active count, or (kDynamic, inside a graph where
+ * the count is unknown at launch) a resident grid whose warps take the next
+ * 32 entries from a counter until the list is done.  The replay pass of the
+ * adjoint (kAdj) sums its alpha gradients per block in shared memory. */
+template <bool kAdj, bool kDynamic>
 __global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting,
-                                                       bool dynamic) {
+                                                       int pass, WfAdjoint A) {
+    __shared__ float s_alpha[kAdj ? RT_ADJ_MAX_ALPHA : 1];
+    if (kAdj) {
+        for (int i = threadIdx.x; i < A.n_alpha; i += blockDim.x) s_alpha[i] = 0.0f;
+        __syncthreads();
+    }
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
-    if (!dynamic) {
+    if (!kDynamic) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
-        return;
+        if (i < n) shade_path<kAdj>(W, W.sorted[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+    } else {
+        const int lane = threadIdx.x & 31;
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&W.ctr->shade_fetch, 32);
+            base = __shfl_sync(kFullWarp, base, 0);
+            if (base >= n) break;
+            const int i = base + lane;
+            if (i < n) shade_path<kAdj>(W, W.sorted[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+            __syncwarp();
+        }
     }
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(&W.ctr->shade_fetch, 32);
-        base = __shfl_sync(kFullWarp, base, 0);
-        if (base >= n) break;
-        const int i = base + lane;
-        if (i < n) shade_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
-        __syncwarp();
+    if (kAdj) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < A.n_alpha; i += blockDim.x)
+            if (s_alpha[i] != 0.0f) atomicAdd(A.grad_alpha + i, s_alpha[i]);
     }
 }
 
@@ -657,9 +723,11 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
 }
 
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
-                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches) {
+                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
+                        int pass, const WfAdjoint* adj) {
     static const int sort_blocks = resident_blocks(k_wf_sort_scatter, 256);
-    static const int shade_blocks = resident_blocks(k_wf_shade, 128);
+    static const int shade_blocks = resident_blocks(k_wf_shade<false, true>, 128);
+    const WfAdjoint A = adj ? *adj : WfAdjoint{-1, 0, nullptr, nullptr, nullptr, nullptr};
     const bool known = n_hint >= 0;
     const int n = known ? std::min(n_hint, W.slots) : W.slots;
     k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
@@ -667,7 +735,9 @@ cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned
         const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
         k_wf_sort_count<<<sb, 256, 0, s>>>(W);
         k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
-        k_wf_shade<<<known ? grid_for(n, 128) : (unsigned)shade_blocks, 128, 0, s>>>(W, status, stats, counting, !known);
+        if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A);
+        else if (pass == WF_PASS_REPLAY) k_wf_shade<true, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
+        else k_wf_shade<false, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
         *launches += 3;
     }
     if (has_loop) k_wf_tail_loop<<<1, 32, 0, s>>>(W, loop, status);

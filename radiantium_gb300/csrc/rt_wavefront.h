@@ -32,6 +32,19 @@ struct WfJob {
     long long count;               /* P.w * P.h * P.chunk_len */
 };
 
+/* the adjoint replay pass (rt_adjoint.cuh): parameters and gradient sums */
+struct WfAdjoint {
+    int albedo_tex;          /* texture whose texels are parameters, or -1 */
+    int n_alpha;
+    const int* alpha_slot;   /* per material: alpha parameter index or -1 */
+    float* grad_albedo;
+    float* grad_alpha;
+    const float* dLdI;       /* crop film layout, already divided by spp */
+};
+/* shade pass of a run: a render, the adjoint's forward pass (per-sample
+ * radiance kept raw, invalid values included), or the adjoint's replay */
+enum { WF_PASS_RENDER = 0, WF_PASS_FORWARD_RAW = 1, WF_PASS_REPLAY = 2 };
+
 /* device counters of a run; iteration i reads active[i & 1] and fills active[(i + 1) & 1] */
 struct WfCounters {
     long long total;               /* samples of the round, all jobs */
@@ -79,6 +92,9 @@ struct WfState {
     float4* ext_hit; int32_t* ext_sub;
     float4* mis_hit; int32_t* mis_sub;
     uint8_t* occluded;
+    /* adjoint replay: d ln (f w) / d alpha of the pending light and BSDF terms,
+     * d ln f / d alpha of the continuation, alpha slot of the pending vertex */
+    float4* adj_rho;
 };
 
 /* Starts the round: every slot takes a camera sample, the first active list
@@ -92,6 +108,7 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
  * it), -1 inside a graph (grids cover every slot, surplus blocks return).
  * Kernel launches are added to *launches. */
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
-                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches);
+                        cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
+                        int pass = WF_PASS_RENDER, const WfAdjoint* adj = nullptr);
 
 #endif

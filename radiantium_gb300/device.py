@@ -101,6 +101,44 @@ class Device:
         p = settings.to_c()
         self._check(self.lib.rt_render_device(self.h, C.byref(p), C.c_void_p(out_ptr), C.c_void_p(stream or None)))
 
+    def adjoint_forward(self, settings: RenderSettings) -> np.ndarray:
+        """The film the gradients refer to (same as render)."""
+        w, h = self._crop(settings)
+        out = np.zeros(w * h * 3, dtype=np.float32)
+        p = settings.to_c()
+        self._check(self.lib.rt_adjoint_forward(self.h, C.byref(p), _ptr(out)))
+        return out.reshape(w, h, 3)
+
+    def adjoint_backward(self, settings: RenderSettings, dl_dimage: np.ndarray, albedo_texture: int = -1,
+                         alpha_materials=()):
+        """Gradient of sum(dl_dimage * I) w.r.t. the albedo texture's texels ((w, h, 3),
+        ColorBuffer layout) and the alpha of each listed material."""
+        w, h = self._crop(settings)
+        dl = np.ascontiguousarray(dl_dimage, dtype=np.float32).reshape(-1)
+        if dl.size != w * h * 3:
+            raise ValueError("dl_dimage must have the crop's w * h * 3 values")
+        mats = np.ascontiguousarray(alpha_materials, dtype=np.int32)
+        desc = N.AdjointDesc(albedo_texture, len(mats), mats.ctypes.data_as(C.POINTER(C.c_int32)))
+        if albedo_texture >= 0:
+            t = self.scene.textures[albedo_texture]
+            g_alb = np.zeros(t.width * t.height * 3, dtype=np.float32)
+        else:
+            t, g_alb = None, np.zeros(3, dtype=np.float32)
+        g_alpha = np.zeros(max(1, len(mats)), dtype=np.float32)
+        p = settings.to_c()
+        self._check(self.lib.rt_adjoint_backward(self.h, C.byref(p), C.byref(desc), _ptr(dl), _ptr(g_alb),
+                                                 _ptr(g_alpha)))
+        return (g_alb.reshape(t.width, t.height, 3) if t is not None else None), g_alpha[:len(mats)]
+
+    def update_texture(self, index: int, data: np.ndarray):
+        """New texels (ColorBuffer layout) for texture `index` of the uploaded scene."""
+        t = self.scene.textures[index]
+        d = np.ascontiguousarray(data, dtype=np.float32).reshape(-1)
+        if d.size != t.width * t.height * 3:
+            raise ValueError("texel count mismatch")
+        self._check(self.lib.rt_update_texture(self.h, index, _ptr(d)))
+        t.data = d.copy()
+
     def render_batch(self, items) -> list:
         """Renders [(Device holding the scene, RenderSettings), ...] as one wavefront
         on this device's context; returns the averaged films (x, y, rgb)."""

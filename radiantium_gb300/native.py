@@ -103,6 +103,11 @@ class RenderParams(C.Structure):
                 ("x0", C.c_int32), ("y0", C.c_int32), ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class AdjointDesc(C.Structure):
+    _fields_ = [("albedo_texture", C.c_int32), ("alpha_count", C.c_int32),
+                ("alpha_materials", C.POINTER(C.c_int32))]
+
+
 class BatchItem(C.Structure):
     _fields_ = [("scene_ctx", C.c_void_p), ("params", RenderParams), ("out_rgb", C.c_void_p)]
 
@@ -138,11 +143,12 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_get_stats", "rt_set_counting",
+    "rt_render", "rt_render_device", "rt_adjoint_forward", "rt_adjoint_backward", "rt_update_texture", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_get_stats", "rt_set_counting",
     "rt_set_renderer", "rt_cancel",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
 MAX_BATCH = 256
+ADJ_MAX_ALPHA = 1024
 MAX_SLOTS = 1 << 21       # path slots in flight (wavefront)
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024   # RT_NOALLOC_SCRATCH_BYTES
 
@@ -179,6 +185,12 @@ def _declare(lib):
     lib.rt_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.rt_set_counting.restype = C.c_int
     lib.rt_set_counting.argtypes = [vp, C.c_int]
+    lib.rt_adjoint_forward.restype = C.c_int
+    lib.rt_adjoint_forward.argtypes = [vp, C.POINTER(RenderParams), vp]
+    lib.rt_adjoint_backward.restype = C.c_int
+    lib.rt_adjoint_backward.argtypes = [vp, C.POINTER(RenderParams), C.POINTER(AdjointDesc), vp, vp, vp]
+    lib.rt_update_texture.restype = C.c_int
+    lib.rt_update_texture.argtypes = [vp, C.c_int, vp]
     lib.rt_render_batch.restype = C.c_int
     lib.rt_render_batch.argtypes = [vp, C.POINTER(BatchItem), C.c_int]
     lib.rt_render_batch_device.restype = C.c_int

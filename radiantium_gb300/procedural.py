@@ -293,6 +293,66 @@ def batch_scenes(count: int = 32, seed: int = 11):
     return [batch_scene(i, seed) for i in range(count)]
 
 
+def albedo_image(size: int, seed: int, lo: float = 0.15, hi: float = 0.85) -> np.ndarray:
+    """size x size x 3 smooth colour field in [lo, hi] (value noise per channel), img[y, x, c]."""
+    ys, xs = np.meshgrid(np.arange(size) / size, np.arange(size) / size, indexing="ij")
+    pts = np.stack([xs.reshape(-1) * 6.0, ys.reshape(-1) * 6.0, np.zeros(size * size)], 1)
+    img = np.empty((size * size, 3))
+    for c in range(3):
+        n = value_noise(pts + 17.0 * c, seed + c)
+        img[:, c] = lo + (hi - lo) * (0.5 + 0.5 * np.clip(n, -1.0, 1.0))
+    return img.reshape(size, size, 3).astype(np.float32)
+
+
+def adjoint_patches(width=256, height=256, sphere_n=129, tex_size=512, patches=(8, 8), seed=5, alpha=None,
+                    albedo_seed=None):
+    """The adjoint workload: the displaced sphere of the instanced workload (one
+    instance, 12 * 129^2 triangles) with spherical UVs, cut into 8 x 8 patches by
+    (theta, phi) of the triangle centroids; each patch is a GGX rough_plastic with
+    its own alpha and the shared albedo texture (tex_size^2 RGB, Clamp/Nearest);
+    Gaussian-lobe environment.  Returns (scene, settings, params) where params
+    holds the albedo texture index and the alpha material indices / values."""
+    rng = np.random.default_rng(seed)
+    s = SceneDesc(camera=Camera.look_at(width, height, 35.0, (0.0, 0.9, 3.6), (0.0, 0.0, 0.0)), name="adjoint")
+    sph = displaced_sphere(sphere_n, 7)
+    p = sph.positions.astype(np.float64)
+    d = p / np.linalg.norm(p, axis=1, keepdims=True)
+    uv = np.stack([np.arctan2(d[:, 0], -d[:, 2]) / (2 * math.pi) + 0.5,
+                   np.arccos(np.clip(d[:, 1], -1, 1)) / math.pi], 1).astype(np.float32)
+    cen = d[sph.indices].mean(1)
+    cen /= np.linalg.norm(cen, axis=1, keepdims=True)
+    th = np.arccos(np.clip(cen[:, 1], -1, 1)) / math.pi
+    ph = np.arctan2(cen[:, 0], -cen[:, 2]) / (2 * math.pi) + 0.5
+    nt, nph = patches
+    patch = np.minimum((th * nt).astype(int), nt - 1) * nph + np.minimum((ph * nph).astype(int), nph - 1)
+    if albedo_seed is None:
+        albedo_seed = seed + 100
+    tex = s.add_texture(Texture.from_image_hw3(albedo_image(tex_size, albedo_seed)))
+    zero = s.add_const(0.0)
+    if alpha is None:
+        alpha = rng.uniform(0.05, 0.5, nt * nph)
+    mats = []
+    for k in range(nt * nph):
+        rough = s.add_const(math.sqrt(float(alpha[k])))
+        m = s.add_material(Material(N.MAT_ROUGH_PLASTIC, N.DIST_GGX, tex_r=tex, tex_roughness=rough,
+                                    tex_anisotropic=zero))
+        mats.append(m)
+        sel = np.nonzero(patch == k)[0]
+        if sel.size == 0:
+            continue
+        tri = sph.indices[sel]
+        used, inv = np.unique(tri.reshape(-1), return_inverse=True)
+        mesh = Mesh(sph.positions[used], inv.reshape(-1, 3).astype(np.int32), None, uv[used])
+        s.groups.append(Group(N.GROUP_MESH, s.add_mesh(mesh), material=m))
+    env = s.add_texture(gaussian_lobe_env(256, 128, seed))
+    s.groups.append(Group(N.GROUP_INFINITE_LIGHT, env))
+    settings = RenderSettings(N.INTEGRATOR_PATH, N.METHOD_MIS, N.STRATEGY_UNIFORM, max_depth=6, min_depth=3,
+                              rr_threshold=0.99, spp=64, seed=1)
+    params = {"albedo_texture": tex, "alpha_materials": mats, "alpha": np.asarray(alpha, dtype=np.float64),
+              "roughness_textures": [s.materials[m].tex_roughness for m in mats]}
+    return s, settings, params
+
+
 WORKLOADS = {
     "cornell": cornell_box,
     "instanced": instanced_spheres,
