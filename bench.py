@@ -20,6 +20,7 @@ all host cores) on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import math
 import json
 import os
 import subprocess
@@ -49,12 +50,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["instanced", "cornell", "volume", "batch"], default="instanced")
+    ap.add_argument("--workload", choices=["instanced", "cornell", "volume", "batch", "adjoint"], default="instanced")
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
+    ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="steps of the plain megakernel timed in the same run for the batched/plain ratio (0: skip)")
     return ap.parse_args()
@@ -62,6 +64,9 @@ def parse():
 
 def workload(name):
     from radiantium_gb300 import procedural
+    if name == "adjoint":
+        scene, st, _ = procedural.adjoint_patches()
+        return scene, st
     scene, st = {"instanced": procedural.instanced_spheres, "cornell": procedural.cornell_box,
                  "volume": procedural.volume_sphere}[name]()
     return scene, st
@@ -72,6 +77,9 @@ def workload_config(name, scene, st, spp_step):
     return {
         "workload": {"instanced": "path MIS, 64 instances of a displaced sphere (GGX conductor / rough dielectric), "
                                   "1024x512 Gaussian-lobe env",
+                     "adjoint": "forward renders of the adjoint workload's scene (64 rough_plastic patches, 512x512 "
+                                "albedo texture): the reference has no derivatives, finite differences need two "
+                                "renders per parameter",
                      "cornell": "path MIS, procedural Cornell box (36 tris, ceiling quad light)",
                      "volume": "vol_path, displaced sphere bounding a homogeneous medium, ground, quad light"}[name],
         "film": [scene.camera.width, scene.camera.height],
@@ -601,8 +609,155 @@ def run_batch(args):
     return 0
 
 
+def adjoint_setup(d, prm, rng_seed=0):
+    """Target film with perturbed albedo (x U[0.7, 1.3]) and alpha (x U[0.7, 1.3])."""
+    import math
+    s = d.scene
+    ti, rts, alpha0 = prm["albedo_texture"], prm["roughness_textures"], prm["alpha"].copy()
+    alb0 = s.textures[ti].data.copy()
+    rng = np.random.default_rng(rng_seed)
+
+    def set_params(alb, alpha):
+        d.update_texture(ti, alb)
+        for t, a in zip(rts, alpha):
+            d.update_texture(t, np.full(3, math.sqrt(a), np.float32))
+    return alb0, alpha0, set_params, (np.clip(alb0 * rng.uniform(0.7, 1.3, alb0.shape), 0.05, 0.95).astype(np.float32),
+                                      alpha0 * rng.uniform(0.7, 1.3, alpha0.shape))
+
+
+def run_adjoint(args):
+    """The adjoint workload: one step = forward film + L2-loss gradient + backward
+    pass to every albedo texel and every patch alpha."""
+    import torch
+    from radiantium_gb300 import procedural
+    from radiantium_gb300.device import Device
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    scene, st, prm = procedural.adjoint_patches()
+    d = Device(local)
+    d.upload(scene)
+    alb0, alpha0, set_params, (alb_t, alpha_t) = adjoint_setup(d, prm)
+    set_params(alb_t, alpha_t)
+    target = d.render(st.replace(spp=4 * st.spp, seed=99))
+    set_params(alb0, alpha0)
+    n_params = alb0.size + len(prm["alpha_materials"])
+    W, H = scene.camera.width, scene.camera.height
+    base = rank * 1000
+
+    def step(i):
+        stx = st.replace(seed=base + i)
+        img = d.render(stx)
+        dl = 2.0 * (img - target)
+        ga, gal = d.adjoint_backward(stx, dl, prm["albedo_texture"], prm["alpha_materials"])
+        return img, ga, gal
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    times, bwd_ms, fwd_times = [], 0.0, []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        stx = st.replace(seed=base + args.warmup + i)
+        img = d.render(stx)
+        t1 = time.perf_counter()
+        dl = 2.0 * (img - target)
+        ga, gal = d.adjoint_backward(stx, dl, prm["albedo_texture"], prm["alpha_materials"])
+        times.append(time.perf_counter() - t0)
+        fwd_times.append(t1 - t0)
+        bwd_ms += d.stats()["render_kernel_ms"]
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_s = float(np.sum(times))
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    s_step = total_s / args.steps
+    samples_step = W * H * st.spp
+    fwd_s = float(np.mean(fwd_times))
+    # finite-difference checks along one direction per parameter group (linearised loss)
+    check = None
+    if not args.no_fd_check:
+        ref = d.render(st.replace(spp=1024, seed=77))
+        w = (2 * (ref - target)).astype(np.float32)
+        lin = lambda stx: float((w.astype(np.float64) * d.render(stx)).sum())
+        sta = st.replace(seed=3)
+        g, _ = d.adjoint_backward(sta, w, prm["albedo_texture"], [])
+        v = np.random.default_rng(1).standard_normal(alb0.shape).astype(np.float32)
+        set_params(alb0 + 1e-3 * v, alpha0); lp = lin(sta)
+        set_params(alb0 - 1e-3 * v, alpha0); lm = lin(sta)
+        set_params(alb0, alpha0)
+        fd_a, ad_a = (lp - lm) / 2e-3, float((g.reshape(-1).astype(np.float64) * v).sum())
+        _, gal = d.adjoint_backward(st.replace(spp=16384, seed=8), w, -1, prm["alpha_materials"])
+        va = np.sign(gal) * alpha0
+        ad_r = float((gal.astype(np.float64) * va).sum())
+        fds = []
+        for k in range(8):
+            stx = st.replace(spp=4096, seed=100 + k)
+            set_params(alb0, alpha0 + 0.01 * va); lp = lin(stx)
+            set_params(alb0, alpha0 - 0.01 * va); lm = lin(stx)
+            fds.append((lp - lm) / 0.02)
+        set_params(alb0, alpha0)
+        fd_r = float(np.mean(fds))
+        check = {"albedo": {"fd": fd_a, "adjoint": ad_a, "rel_err": abs(fd_a - ad_a) / abs(fd_a),
+                            "how": "random normal direction over all texels, eps 1e-3, common random numbers, 64 spp"},
+                 "alpha": {"fd": fd_r, "fd_stderr": float(np.std(fds, ddof=1) / math.sqrt(len(fds))), "adjoint": ad_r,
+                           "rel_err": abs(fd_r - ad_r) / abs(fd_r),
+                           "how": "direction sign(grad) x alpha, eps 1 %, mean of 8 seeds x 4096 spp (common random "
+                                  "numbers) vs adjoint at 16384 spp"},
+                 "loss": "linearised L2: sum(w * I), w = 2 (I_1024spp - target)"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, st, args.cpu_seconds)
+        cpu["sample"] = ("forward renders of the oracle (the reference has no derivatives: finite differences "
+                         "need two renders per parameter): " + cpu["sample"])
+    line = {
+        "metric": METRIC, "value": samples_step * world / s_step, "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * s_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": "adjoint: displaced sphere (one instance, 199,692 triangles) in 64 rough_plastic "
+                               "patches sharing a 512x512 albedo texture, Gaussian-lobe env; path MIS; L2 loss "
+                               "against a film of perturbed parameters",
+                   "film": [W, H], "spp": st.spp, "max_depth": st.max_depth, "parameters": int(n_params),
+                   "step": "forward render + dL/dI + backward (gradient w.r.t. all parameters)",
+                   "parallelism": f"replicas x{world}", "l2": "inputs resident; no flush (forward and backward "
+                   "re-read the scene)"},
+        "adjoint": {"grads_per_s": world / s_step, "params_per_s": n_params * world / s_step,
+                    "backward_ms": bwd_ms / args.steps, "forward_ms": 1000.0 * fwd_s,
+                    "fd_params_per_s": 1.0 / (2.0 * fwd_s),
+                    "vs_fd": (n_params / s_step) / (1.0 / (2.0 * fwd_s)),
+                    "fd_check": check},
+        "cpu_baseline": cpu,
+        "e2e": {"value": samples_step * world / s_step, "unit": "samples/s", "h2d_bytes_per_step": W * H * 12,
+                "d2h_bytes_per_step": W * H * 12 + int(n_params) * 4,
+                "note": "the step is timed end to end through the C ABI: film to host, dL/dI from host, gradients to host"},
+        "gpu_launches": None,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    d.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "adjoint":
+        if args.impl == "reference":
+            return run_reference(args)
+        return run_adjoint(args)
     if args.workload == "batch":
         return run_batch_reference(args) if args.impl == "reference" else run_batch(args)
     if args.impl == "reference":
