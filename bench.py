@@ -493,6 +493,13 @@ def run_batch(args):
 
     samples_step = sum(s.camera.width * s.camera.height * st.spp
                        for (s, _), st in zip(scenes, batch_step_settings(scenes, 0)))
+    tuned = None
+    if args.renderer == "auto":
+        host.set_renderer(N.RENDERER_AUTO)
+        probe = [(d, st.replace(spp=max(1, st.spp // 4), sample_begin=10 ** 6)) for d, st in items(0)]
+        tuned = host.autotune(probe)
+        mode = N.RENDERER_WAVEFRONT_GRAPH if tuned["renderer"] == N.RENDERER_WAVEFRONT_GRAPH else N.RENDERER_WAVEFRONT
+        host.set_renderer(mode)
     host.set_counting(True)
     host.render_batch_device(items(0), ptrs, stream)
     counts = host.stats()
@@ -583,7 +590,8 @@ def run_batch(args):
                        parallelism=f"replicas x{world} (independent sample passes)",
                        l2="256 MiB flush between timed steps (outside the CUDA events)",
                        renderer="batched wavefront, bounce loop as a CUDA graph while-loop" if graph
-                       else "batched wavefront, bounce loop driven from the host"),
+                       else "batched wavefront, bounce loop driven from the host",
+                       autotune=tuned),
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,

@@ -371,6 +371,24 @@ int rt_render_batch(void* ctx, const rt_batch_item* items, int n);
  * context stream); returns once the films are written. */
 int rt_render_batch_device(void* ctx, const rt_batch_item* items, int n, void* stream);
 
+/* Settings chosen by rt_autotune. */
+typedef struct rt_tune_result {
+    int32_t capacity;      /* path slots in flight */
+    int32_t refill;        /* idle lanes of a trace warp before it fetches new rays */
+    int32_t renderer;      /* RT_RENDERER_WAVEFRONT or RT_RENDERER_WAVEFRONT_GRAPH */
+    float ms;              /* probe time of the chosen settings */
+    float ms_default;      /* probe time of the defaults (2 Mi slots, refill 8, host-driven loop) */
+} rt_tune_result;
+
+/* Renders the batch (rt_render_batch, films into the items' outputs) under
+ * each combination of the wavefront settings that do not change a film -
+ * path slots in flight (2 Mi, 1 Mi, 512 Ki), trace-warp refill threshold
+ * (4, 8, 16 idle lanes) and host- or graph-driven bounce loop - and keeps
+ * the fastest on this context for later renders and batches (the loop
+ * driver applies under RT_RENDERER_AUTO).  Probe with a representative,
+ * short batch (a few spp).  No counterpart in the reference. */
+int rt_autotune(void* ctx, const rt_batch_item* items, int n, rt_tune_result* out);
+
 /* Requests cancellation of a running render (Renderer.Stop, BlockBasedRenderer.cs:85-88). */
 int rt_cancel(void* ctx);
 

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -91,6 +92,8 @@ struct Ctx {
     WfJob* d_jobs = nullptr;                   /* device job table (WF_MAX_JOBS entries) */
     WfJob* h_jobs = nullptr;                   /* pinned staging of the job table */
     int wf_capacity = WF_MAX_SLOTS;            /* path slots in flight */
+    int wf_refill = 8;                         /* idle lanes before a trace warp fetches (1..32) */
+    bool wf_graph_pref = false;                /* RT_RENDERER_AUTO drives the wavefront as a graph */
     uint64_t wf_generation = 0;                /* bumped whenever the path-state buffers move */
     /* the bounce loop captured as a CUDA graph while-loop */
     cudaGraph_t wf_graph = nullptr;
@@ -796,7 +799,8 @@ struct WfJobIn {
  * condition when no path is left.  Rebuilt when the path state moves or the
  * counting mode changes. */
 void ensure_wf_graph(Ctx* c, const WfState& W) {
-    const uint64_t key = (c->wf_generation << 24) ^ ((uint64_t)W.slots << 1) ^ (c->counting ? 1u : 0u);
+    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 7) ^ ((uint64_t)W.refill << 1) ^
+                         (c->counting ? 1u : 0u);
     if (c->wf_exec && c->wf_graph_key == key) return;
     if (c->wf_exec) { cudaGraphExecDestroy(c->wf_exec); c->wf_exec = nullptr; }
     if (c->wf_graph) { cudaGraphDestroy(c->wf_graph); c->wf_graph = nullptr; }
@@ -871,6 +875,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         WfState W = c->wf;
         W.slots = slots;
         W.shadow_base = 2 * slots;
+        W.refill = c->wf_refill;
         /* one pass over the round's samples: start every slot, bounce until no path is left */
         auto run_pass = [&](int pass) {
             std::memset(c->h_ctr, 0, sizeof(WfCounters));
@@ -941,7 +946,8 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     jobs[0].view = c->d_view;
     jobs[0].P = P;
     jobs[0].film = c->film;
-    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH);
+    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH ||
+                              (c->renderer == RT_RENDERER_AUTO && c->wf_graph_pref));
 }
 
 /* rt_render_batch(_device): every item's film through one wavefront run;
@@ -983,7 +989,8 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
-    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH);
+    wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH ||
+                              (c->renderer == RT_RENDERER_AUTO && c->wf_graph_pref));
     uint64_t samples = 0;
     for (int i = 0; i < n; i++) {
         const int64_t npix = (int64_t)jobs[i].P.w * jobs[i].P.h;
@@ -1107,6 +1114,43 @@ void update_texture(Ctx* c, int tex, const float* texels) {
     CK(cudaMemcpyAsync((void*)(c->view.texels + t.offset), texels, (size_t)t.width * t.height * 12, cudaMemcpyHostToDevice,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
+}
+
+/* rt_autotune: times the caller's batch under each setting that leaves films
+ * unchanged (path slots in flight, trace-warp refill threshold, host- or
+ * graph-driven bounce loop) and keeps the fastest on the context */
+void autotune(Ctx* c, const rt_batch_item* items, int n, rt_tune_result* out) {
+    if (!items || n <= 0 || !out) throw RtFail(RT_ERR_INVALID_ARG, "autotune: no items or no result");
+    const int caps[] = {WF_MAX_SLOTS, WF_MAX_SLOTS / 2, WF_MAX_SLOTS / 4};
+    const int refills[] = {8, 4, 16};
+    const int modes[] = {RT_RENDERER_WAVEFRONT, RT_RENDERER_WAVEFRONT_GRAPH};
+    const int keep_cap = c->wf_capacity, keep_refill = c->wf_refill, keep_mode = c->renderer;
+    const bool keep_pref = c->wf_graph_pref;
+    auto probe = [&](int cap, int refill, int mode) {
+        c->wf_capacity = cap; c->wf_refill = refill; c->renderer = mode;
+        render_batch(c, items, n, false, nullptr);               /* warm: buffers, graph */
+        const auto t0 = std::chrono::steady_clock::now();
+        render_batch(c, items, n, false, nullptr);
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    double best = 1e300, base = 0;
+    int bc = keep_cap, br = keep_refill, bm = RT_RENDERER_WAVEFRONT;
+    try {
+        for (int mode : modes)
+            for (int cap : caps)
+                for (int refill : refills) {
+                    const double ms = probe(cap, refill, mode);
+                    if (mode == RT_RENDERER_WAVEFRONT && cap == WF_MAX_SLOTS && refill == 8) base = ms;
+                    if (ms < best) { best = ms; bc = cap; br = refill; bm = mode; }
+                }
+    } catch (...) {
+        c->wf_capacity = keep_cap; c->wf_refill = keep_refill; c->renderer = keep_mode; c->wf_graph_pref = keep_pref;
+        throw;
+    }
+    c->wf_capacity = bc; c->wf_refill = br; c->renderer = keep_mode;
+    c->wf_graph_pref = bm == RT_RENDERER_WAVEFRONT_GRAPH;
+    out->capacity = bc; out->refill = br; out->renderer = bm;
+    out->ms = (float)best; out->ms_default = (float)base;
 }
 
 void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
@@ -1255,6 +1299,10 @@ int rt_adjoint_backward(void* ctx, const rt_render_params* params, const rt_adjo
 int rt_update_texture(void* ctx, int texture, const float* texels) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { update_texture(c, texture, texels); });
+}
+int rt_autotune(void* ctx, const rt_batch_item* items, int n, rt_tune_result* out) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { autotune(c, items, n, out); });
 }
 int rt_render_batch(void* ctx, const rt_batch_item* items, int n) {
     Ctx* c = (Ctx*)ctx;

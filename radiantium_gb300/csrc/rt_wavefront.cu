@@ -157,12 +157,11 @@ __global__ void __launch_bounds__(256) k_wf_start(WfState W) {
 
 /* Persistent traversal with dynamic ray fetch (Aila & Laine 2009): each warp
  * keeps its lanes busy by handing a new queue entry to every lane whose ray
- * has finished, as soon as kRefill lanes are idle, instead of idling until
+ * has finished, as soon as W.refill lanes are idle, instead of idling until
  * the warp's longest ray is done.  The traversal is the step machine of
  * TravClosest / TravAny, so a lane can take a new ray between any two steps
  * and the per-ray results are the same as a one-ray-per-thread launch. */
 constexpr unsigned kFullWarp = 0xffffffffu;
-constexpr int kRefill = 8;
 
 /* One warp-wide fetch: returns this lane's queue entry (>= n: none) and sets
  * `exhausted` (warp-uniform) once the queue has been handed out. */
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(128) k_wf_trace_closest(WfState W, uint32_t* s
         const unsigned idle = __ballot_sync(kFullWarp, item < 0);
         if (exhausted) {
             if (idle == kFullWarp) break;
-        } else if (__popc(idle) >= kRefill) {
+        } else if (__popc(idle) >= W.refill) {
             const int q = fetch_entry(&W.ctr->fetch[0], n, idle, &exhausted);
             if (item < 0 && q < n) {
                 meta = W.q_meta[q];
@@ -238,7 +237,7 @@ __global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t*
         const unsigned idle = __ballot_sync(kFullWarp, item < 0);
         if (exhausted) {
             if (idle == kFullWarp) break;
-        } else if (__popc(idle) >= kRefill) {
+        } else if (__popc(idle) >= W.refill) {
             const int e = fetch_entry(&W.ctr->fetch[1], n, idle, &exhausted);
             if (item < 0 && e < n) {
                 const int q = W.shadow_base + e;

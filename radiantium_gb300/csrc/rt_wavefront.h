@@ -68,6 +68,7 @@ struct WfState {
     float4* q_o; float4* q_d; int32_t* q_meta;
     int32_t shadow_base;
     int32_t slots;
+    int32_t refill;          /* idle lanes of a trace warp before it fetches new rays */
     WfCounters* ctr;
     const WfJob* jobs;
     /* active slot lists by iteration parity, and the list regrouped by shade key */

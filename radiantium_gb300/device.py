@@ -139,6 +139,22 @@ class Device:
         self._check(self.lib.rt_update_texture(self.h, index, _ptr(d)))
         t.data = d.copy()
 
+    def autotune(self, items) -> dict:
+        """Picks the fastest film-preserving wavefront settings for this batch
+        (rt_autotune); they stay on this context."""
+        outs, arr = [], (N.BatchItem * len(items))()
+        for i, (d, st) in enumerate(items):
+            w, h = d._crop(st)
+            out = np.zeros(w * h * 3, dtype=np.float32)
+            outs.append(out)
+            arr[i].scene_ctx = d.h
+            arr[i].params = st.to_c()
+            arr[i].out_rgb = out.ctypes.data
+        r = N.TuneResult()
+        self._check(self.lib.rt_autotune(self.h, arr, len(items), C.byref(r)))
+        return {"capacity": r.capacity, "refill": r.refill, "renderer": r.renderer, "ms": r.ms,
+                "ms_default": r.ms_default}
+
     def render_batch(self, items) -> list:
         """Renders [(Device holding the scene, RenderSettings), ...] as one wavefront
         on this device's context; returns the averaged films (x, y, rgb)."""

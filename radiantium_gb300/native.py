@@ -112,6 +112,11 @@ class BatchItem(C.Structure):
     _fields_ = [("scene_ctx", C.c_void_p), ("params", RenderParams), ("out_rgb", C.c_void_p)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("capacity", C.c_int32), ("refill", C.c_int32), ("renderer", C.c_int32), ("ms", C.c_float),
+                ("ms_default", C.c_float)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64),
                 ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64), ("instance_visits", C.c_uint64),
@@ -143,7 +148,7 @@ LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
-    "rt_render", "rt_render_device", "rt_adjoint_forward", "rt_adjoint_backward", "rt_update_texture", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_get_stats", "rt_set_counting",
+    "rt_render", "rt_render_device", "rt_adjoint_forward", "rt_adjoint_backward", "rt_update_texture", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_autotune", "rt_get_stats", "rt_set_counting",
     "rt_set_renderer", "rt_cancel",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
@@ -191,6 +196,8 @@ def _declare(lib):
     lib.rt_adjoint_backward.argtypes = [vp, C.POINTER(RenderParams), C.POINTER(AdjointDesc), vp, vp, vp]
     lib.rt_update_texture.restype = C.c_int
     lib.rt_update_texture.argtypes = [vp, C.c_int, vp]
+    lib.rt_autotune.restype = C.c_int
+    lib.rt_autotune.argtypes = [vp, C.POINTER(BatchItem), C.c_int, C.POINTER(TuneResult)]
     lib.rt_render_batch.restype = C.c_int
     lib.rt_render_batch.argtypes = [vp, C.POINTER(BatchItem), C.c_int]
     lib.rt_render_batch_device.restype = C.c_int

@@ -120,3 +120,22 @@ def test_batch_rejects_unsupported_items(scenes):
         assert e.value.code == N.RT_ERR_INVALID_ARG
     finally:
         host.close()
+
+
+def test_autotune_keeps_films(scenes):
+    """rt_autotune only picks settings that leave films unchanged: a batch
+    rendered after tuning equals the one-scene megakernel renders."""
+    items = _items(scenes)
+    want = _singles(items)
+    host = Device(0)
+    try:
+        r = host.autotune([(d, st.replace(spp=1)) for d, st in items])
+        assert r["capacity"] in (N.MAX_SLOTS, N.MAX_SLOTS // 2, N.MAX_SLOTS // 4)
+        assert r["refill"] in (4, 8, 16)
+        assert r["renderer"] in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH)
+        assert 0 < r["ms"] <= r["ms_default"]
+        got = host.render_batch(items)
+        for g, w in zip(got, want):
+            assert np.array_equal(_bits(g), _bits(w))
+    finally:
+        host.close()
