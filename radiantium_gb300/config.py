@@ -386,6 +386,7 @@ class RendererBuilder:
             self.global_medium_cfg = self.camera_cfg.sub("medium")
         if cfg.has("accel"):
             self.accel_cfg = cfg.sub("accel")
+        self.output_cfg = cfg.sub("output") if cfg.has("output") else None
         for a in cfg.subs("assets"):
             t = a.str("type", None)
             if t == "model":
@@ -550,8 +551,17 @@ class RendererBuilder:
 
 def load_scene_file(path: str, device: int = 0) -> GpuRenderer:
     """Equivalent of the reference CLI's GetRenderer for one JSON scene file."""
+    return load_scene_file_with_output(path, device)[0]
+
+
+def load_scene_file_with_output(path: str, device: int = 0):
+    """GetRenderer (Radiantium.Cli/Program.cs:25-142) with its ResultOutput:
+    (renderer, output); after Wait(), output.save(renderer) writes the files."""
+    from .output import ResultOutput
     with open(path) as f:
         cfg = ConfigParams(json.load(f))
     b = RendererBuilder(os.path.dirname(os.path.abspath(path)),
                         os.path.splitext(os.path.basename(path))[0]).set_default_builders()
-    return b.load(cfg).build(device)
+    b.load(cfg)
+    out = ResultOutput.from_config(getattr(b, "output_cfg", None), b.search_path, b.workspace)
+    return b.build(device), out

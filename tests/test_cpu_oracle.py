@@ -237,3 +237,41 @@ def test_camera_centre_ray_points_at_target():
     d = rays["d"][0]
     assert np.allclose(d, [0, 0, -1], atol=2e-3)
     assert rays["min_t"][0] > 0 and rays["max_t"][0] > 100
+
+
+# ---- film output (ResultOutput) ----------------------------------------------------------
+def test_film_output_formats(tmp_path):
+    import struct
+    import zlib
+    from radiantium_gb300.output import ResultOutput, save_exr, save_pfm, save_png
+    rng = np.random.default_rng(0)
+    film = rng.uniform(0, 2, (5, 3, 3)).astype(np.float32)       # (x, y, rgb)
+    save_pfm(film, str(tmp_path / "a.pfm"))
+    raw = open(tmp_path / "a.pfm", "rb").read()
+    head, data = raw[:raw.index(b"-1.0\n") + 5], raw[raw.index(b"-1.0\n") + 5:]
+    assert head == b"PF\n5 3\n-1.0\n"
+    img = np.frombuffer(data, "<f4").reshape(3, 5, 3)[::-1]
+    assert np.array_equal(img, film.transpose(1, 0, 2))
+    save_png(film, str(tmp_path / "a.png"))
+    png = open(tmp_path / "a.png", "rb").read()
+    assert png[:8] == b"\x89PNG\r\n\x1a\n" and png[12:16] == b"IHDR"
+    w, h = struct.unpack(">II", png[16:24])
+    assert (w, h) == (5, 3)
+    idat = png[png.index(b"IDAT") + 4: png.index(b"IEND") - 8]
+    rows = zlib.decompress(idat)
+    px = np.frombuffer(rows, np.uint8).reshape(3, 1 + 5 * 4)[:, 1:].reshape(3, 5, 4)
+    assert np.array_equal(px[..., :3], np.rint(np.clip(film.transpose(1, 0, 2), 0, 1) * 255).astype(np.uint8))
+    assert (px[..., 3] == 255).all()
+    save_exr(film, str(tmp_path / "a.exr"))
+    exr = open(tmp_path / "a.exr", "rb").read()
+    assert struct.unpack("<ii", exr[:8]) == (20000630, 2)
+    # last scanline: y, byte count, then B, G, R planes of float32
+    line = 8 + 5 * 3 * 4
+    y, n = struct.unpack("<ii", exr[-line:-line + 8])
+    assert (y, n) == (2, 60)
+    planes = np.frombuffer(exr[-line + 8:], "<f4").reshape(3, 5)
+    assert np.array_equal(planes[::-1].T, film[:, 2, :])
+    class R:
+        RenderTarget = film
+    paths = ResultOutput(True, False, True, str(tmp_path), "scene").save(R)
+    assert [os.path.basename(p) for p in paths] == ["scene.png", "scene.exr"]
