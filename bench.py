@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
     ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the converged render for relMSE")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="steps of the plain megakernel timed in the same run for the batched/plain ratio (0: skip)")
     return ap.parse_args()
@@ -268,6 +269,7 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     step_ms, kernel_ms, shade_ms, launches, render_launches = [], 0.0, 0.0, 0, 0
+    frame = torch.zeros_like(film)
     for i in range(args.steps):
         flush.fill_(float(i))  # L2 flush between timed steps, outside the events
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -277,6 +279,7 @@ def run_ours(args):
         e1.record()
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
+        frame += film                          # the steps' passes average to the frame (outside the events)
         s = dev.stats()
         kernel_ms += s["render_kernel_ms"]
         shade_ms += s["shade_kernel_ms"]
@@ -294,6 +297,20 @@ def run_ours(args):
     ms_step = total_ms / args.steps
     samples_step = npix * spp_step
     value = samples_step * world / (ms_step / 1000.0)
+
+    # relMSE of the frame the timed steps rendered, against an independent render
+    # at 8x its spp (SURVEY's converged-reference comparison; films of every
+    # renderer here are identical per sample, so equal spp means equal relMSE)
+    relmse = None
+    if not args.no_relmse:
+        frame_spp = spp_step * args.steps
+        ref = torch.empty_like(film)
+        dev.render_device(st.replace(spp=8 * frame_spp, sample_begin=0, seed=st.seed + 7919), ref.data_ptr(), stream)
+        torch.cuda.synchronize()
+        x, r = (frame / args.steps).double(), ref.double()
+        relmse = {"value": float((((x - r) ** 2) / (r ** 2 + 1e-2)).mean().item()), "frame_spp": frame_spp,
+                  "reference_spp": 8 * frame_spp,
+                  "definition": "mean over pixels and channels of (x - r)^2 / (r^2 + 0.01); r independent seeds"}
 
     # e2e: the C ABI call a host binding makes, film copied to pinned host memory each step
     e2e = None
@@ -365,6 +382,7 @@ def run_ours(args):
                      "launches_per_step": launches_per_step,
                      "kernel_ms_per_step": kernel_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
         "plain_megakernel": plain,
+        "relmse": relmse,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,

@@ -187,7 +187,7 @@ DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
 }
 
 /* closest-hit rays: extension and MIS rays (queue [0, n_closest)) */
-__global__ void __launch_bounds__(128) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
+__global__ void __launch_bounds__(128, 6) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
                                                             bool counting) {
     const int n = min(W.ctr->n_closest, 2 * W.slots);
     int2 stack[2 * RT_STACK_SIZE];
