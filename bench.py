@@ -82,7 +82,8 @@ def workload_config(name, scene, st, spp_step):
                                 "albedo texture): the reference has no derivatives, finite differences need two "
                                 "renders per parameter",
                      "cornell": "path MIS, procedural Cornell box (36 tris, ceiling quad light)",
-                     "volume": "vol_path, displaced sphere bounding a homogeneous medium, ground, quad light"}[name],
+                     "volume": "vol_path, displaced sphere (499,392 triangles) bounding a homogeneous medium, ground, "
+                               "quad light"}[name],
         "film": [scene.camera.width, scene.camera.height],
         "spp_frame": st.spp,
         "spp_per_step": spp_step,
@@ -242,7 +243,7 @@ def run_ours(args):
             "graph": N.RENDERER_WAVEFRONT_GRAPH}[args.renderer]
     dev.set_renderer(mode)
     uses_wavefront = mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) or (
-        mode == N.RENDERER_AUTO and st.integrator == N.INTEGRATOR_PATH and st.strategy == N.STRATEGY_UNIFORM)
+        mode == N.RENDERER_AUTO and st.strategy == N.STRATEGY_UNIFORM)
     upload_s = time.perf_counter() - t0
     W, H = scene.camera.width, scene.camera.height
     npix = W * H

@@ -334,8 +334,8 @@ int rt_get_stats(void* ctx, rt_stats* out);
 int rt_set_counting(void* ctx, int enabled);
 
 /* Selects the render pipeline: RT_RENDERER_AUTO (wavefront where it applies,
- * i.e. the `path` integrator with the Uniform light strategy; megakernel
- * otherwise), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
+ * i.e. the `path` and `vol_path` integrators with the Uniform light
+ * strategy; megakernel otherwise), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
  * driven by the host, with per-phase timings in rt_stats) or
  * RT_RENDERER_WAVEFRONT_GRAPH (bounce loop as one CUDA graph launch per
  * round of samples).  All produce identical films; this is the

@@ -176,6 +176,12 @@ void ensure_wf(Ctx* c, int slots) {
     W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
     W.occluded = wf_alloc<uint8_t>(c, n);
     W.adj_rho = wf_alloc<float4>(c, n);
+    W.vol_env = wf_alloc<int32_t>(c, n);
+    W.trw_start = wf_alloc<float4>(c, n); W.trw_end = wf_alloc<float4>(c, n);
+    W.trw_dir = wf_alloc<float4>(c, n); W.trw_tr = wf_alloc<float4>(c, n);
+    W.itw_o = wf_alloc<float4>(c, n); W.itw_d = wf_alloc<float4>(c, n); W.itw_tr = wf_alloc<float4>(c, n);
+    W.vol_li = wf_alloc<float4>(c, n);
+    W.trw_hit = wf_alloc<float4>(c, n); W.trw_sub = wf_alloc<int32_t>(c, n);
     if (!c->d_ctr) CK(cudaMalloc((void**)&c->d_ctr, sizeof(WfCounters)));
     if (!c->h_ctr) CK(cudaMallocHost((void**)&c->h_ctr, sizeof(WfCounters)));
     if (!c->d_jobs) CK(cudaMalloc((void**)&c->d_jobs, WF_MAX_JOBS * sizeof(WfJob)));
@@ -671,10 +677,10 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
-    const bool uniform_path = P.integrator == RT_INTEGRATOR_PATH && P.strategy == RT_STRATEGY_UNIFORM;
+    const bool uniform_path = P.strategy == RT_STRATEGY_UNIFORM;   /* path or vol_path */
     const bool wavefront = c->renderer == RT_RENDERER_WAVEFRONT || c->renderer == RT_RENDERER_WAVEFRONT_GRAPH;
     if (wavefront && !uniform_path)
-        throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs the path integrator with the Uniform light strategy");
+        throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs the Uniform light strategy");
     if (wavefront || (c->renderer == RT_RENDERER_AUTO && uniform_path)) {
         render_wavefront(c, P, chunk, npix, s);
     } else {
@@ -798,9 +804,9 @@ struct WfJobIn {
  * (trace, phase, sort, shade, tail); the tail kernel clears the loop's
  * condition when no path is left.  Rebuilt when the path state moves or the
  * counting mode changes. */
-void ensure_wf_graph(Ctx* c, const WfState& W) {
-    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 7) ^ ((uint64_t)W.refill << 1) ^
-                         (c->counting ? 1u : 0u);
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol) {
+    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 8) ^ ((uint64_t)W.refill << 2) ^
+                         ((uint64_t)vol << 1) ^ (c->counting ? 1u : 0u);
     if (c->wf_exec && c->wf_graph_key == key) return;
     if (c->wf_exec) { cudaGraphExecDestroy(c->wf_exec); c->wf_exec = nullptr; }
     if (c->wf_graph) { cudaGraphDestroy(c->wf_graph); c->wf_graph = nullptr; }
@@ -818,7 +824,8 @@ void ensure_wf_graph(Ctx* c, const WfState& W) {
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     uint64_t launches = 0;
     cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream);
-    cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches);
+    cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches,
+                                 WF_PASS_RENDER, nullptr, vol);
     cudaGraph_t captured = nullptr;
     CK(cudaStreamEndCapture(c->stream, &captured));
     CK(e1);
@@ -836,6 +843,12 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                    const WfAdjoint* adj = nullptr) {
     if (jobs.empty() || jobs.size() > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "wavefront: 1 to 256 jobs per run");
     std::vector<int> done(jobs.size(), 0);
+    /* one integrator per run: the vol_path shade kernel or the path one */
+    const bool vol = jobs[0].P.integrator == RT_INTEGRATOR_VOL_PATH;
+    for (const WfJobIn& J : jobs)
+        if ((J.P.integrator == RT_INTEGRATOR_VOL_PATH) != vol)
+            throw RtFail(RT_ERR_UNSUPPORTED, "wavefront: a run renders one integrator");
+    if (vol && adj) throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: the path integrator is differentiated");
     ensure_events(c, 4);
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
@@ -885,7 +898,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             CK(rt_wf_start(W, s));
             launches += 2;
             if (use_graph && pass == WF_PASS_RENDER) {
-                ensure_wf_graph(c, W);
+                ensure_wf_graph(c, W, vol);
                 CK(cudaEventRecord(c->events[0], s));
                 CK(cudaGraphLaunch(c->wf_exec, s));
                 CK(cudaEventRecord(c->events[1], s));
@@ -909,7 +922,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaEventRecord(c->events[2], s));
                 CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
-                               s, &launches, pass, adj));
+                               s, &launches, pass, adj, vol));
                 CK(cudaEventRecord(c->events[3], s));
                 launches += 2;
                 trace_launches += 2;

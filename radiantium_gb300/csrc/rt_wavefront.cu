@@ -49,6 +49,9 @@ enum : uint32_t {
     F_DZERO = 32u,       /* pending direct term is exactly zero (no light / no estimate) */
     F_DONE = 64u,        /* the path ends once its pending term is added */
     F_EXT = 128u,        /* an extension ray was enqueued */
+    F_WTR = 256u,        /* vol_path: a Transmittance-walk segment is being traced */
+    F_WIT = 512u,        /* vol_path: an IntersectTr-walk segment is being traced */
+    F_CONT = 1024u,      /* vol_path: the next extension ray waits for the pending term */
 };
 
 DF void warp_add64(unsigned long long* dst, uint32_t v) {
@@ -143,6 +146,7 @@ DF bool start_path(const WfState& W, int slot, bool take) {
     W.rad[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     W.bounce[slot] = make_int2(0, 0);
     W.flags[slot] = F_ALIVE | F_SPECULAR | F_EXT;
+    W.vol_env[slot] = J.view->global_medium;
     W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
     W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
     push_ray(W, q, slot, WF_RAY_EXT, ray);
@@ -182,8 +186,10 @@ DF Ray queued_ray(const WfState& W, int q) {
 DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
     const int path = meta_path(meta);
     const float4 h = make_float4(T.best.t, T.best.u, T.best.v, __int_as_float(T.any ? T.best.slot : -1));
-    if (meta_kind(meta) == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = T.best.sub; }
-    else { W.mis_hit[path] = h; W.mis_sub[path] = T.best.sub; }
+    const int kind = meta_kind(meta);
+    if (kind == WF_RAY_EXT) { W.ext_hit[path] = h; W.ext_sub[path] = T.best.sub; }
+    else if (kind == WF_RAY_MIS) { W.mis_hit[path] = h; W.mis_sub[path] = T.best.sub; }
+    else { W.trw_hit[path] = h; W.trw_sub[path] = T.best.sub; }
 }
 
 /* closest-hit rays: extension and MIS rays (queue [0, n_closest)) */
@@ -564,6 +570,366 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
     }
 }
 
+/* ---- vol_path (VolumetricPathTracer.Li, Integrators/VolumetricPathTracer.cs) ----
+ * A bounce draws all of its random numbers in one shade, in the reference's
+ * order: medium distance, light choice and sample, phase / BSDF sample of
+ * the direct term, continuation, Russian roulette.  The boundary walks of
+ * the direct term (Scene.Transmittance towards the light sample,
+ * Scene.IntersectTr along the phase / BSDF sample) draw none; each of their
+ * segments is one closest-hit ray, traced in later iterations while the
+ * path waits.  When both walks are done the direct term is added, then the
+ * continuation ray (already sampled) is enqueued, so radiance accumulates
+ * in the reference's order. */
+
+DF int pack_env(int env, int count) { return (count << 16) | ((env + 1) & 0xFFFF); }
+DF int env_of(int packed) { return (packed & 0xFFFF) - 1; }
+DF int count_of(int packed) { return packed >> 16; }
+
+/* next Transmittance segment from the walk's current start; false: walk over */
+DF bool trw_push(const WfState& W, int slot) {
+    const float4 st = W.trw_start[slot], en = W.trw_end[slot], dr = W.trw_dir[slot];
+    const V3 start = v3(st.x, st.y, st.z), to = v3(en.x, en.y, en.z);
+    const float dis = Length(to - start);
+    if (dis < 0.0001f) return false;
+    const int q = warp_append(&W.ctr->n_closest, true);
+    push_ray(W, q, slot, WF_RAY_TRW, mkray(start, v3(dr.x, dr.y, dr.z), 0.0001f, dis - 0.0001f));
+    return true;
+}
+/* Scene.Transmittance (Scene.cs:72-103), one traced segment; true: continues */
+DF bool trw_step(const RtSceneView* S, const WfState& W, int slot) {
+    float4 st = W.trw_start[slot], en = W.trw_end[slot];
+    const float4 dr = W.trw_dir[slot], trv = W.trw_tr[slot];
+    V3 start = v3(st.x, st.y, st.z);
+    const V3 to = v3(en.x, en.y, en.z), dir = v3(dr.x, dr.y, dr.z);
+    int env = __float_as_int(st.w), count = __float_as_int(en.w);
+    const float dis = Length(to - start);
+    const Ray ray = mkray(start, dir, 0.0001f, dis - 0.0001f);
+    Isect inct;
+    const bool anyHit = load_hit(S, ray, W.trw_hit[slot], W.trw_sub[slot], &inct);
+    C3 tr = c3(trv.x, trv.y, trv.z);
+    bool more = true;
+    if (anyHit && HasSurface(S, inct)) { tr = c3s(0.0f); more = false; }
+    else {
+        if (env >= 0) tr = tr * MedTr(S->media[env], ray);
+        if (!anyHit) more = false;
+        else {
+            start = inct.P;
+            env = GetMedium(S, inct, dir);
+            if (++count >= RT_WALK_CAP) more = false;
+        }
+    }
+    W.trw_tr[slot] = make_float4(tr.r, tr.g, tr.b, 0.0f);
+    if (!more) return false;
+    W.trw_start[slot] = make_float4(start.x, start.y, start.z, __int_as_float(env));
+    W.trw_end[slot] = make_float4(to.x, to.y, to.z, __int_as_float(count));
+    return trw_push(W, slot);
+}
+DF void itw_push(const WfState& W, int slot, const Ray& r) {
+    const int q = warp_append(&W.ctr->n_closest, true);
+    push_ray(W, q, slot, WF_RAY_MIS, r);
+}
+/* Scene.IntersectTr (Scene.cs:105-131), one traced segment; true: continues.
+ * When over, itw_o holds the radiance found (light-identity check of
+ * EstimateDirect, or the environment on a miss) and itw_tr the throughput. */
+DF bool itw_step(const RtSceneView* S, const WfState& W, int slot, int light, V3 wle) {
+    const float4 o = W.itw_o[slot], d = W.itw_d[slot], trv = W.itw_tr[slot];
+    Ray ray = mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w);
+    const int packed = __float_as_int(trv.w);
+    int env = env_of(packed), count = count_of(packed);
+    C3 tr = c3(trv.x, trv.y, trv.z);
+    Isect inct;
+    const bool anyHit = load_hit(S, ray, W.mis_hit[slot], W.mis_sub[slot], &inct);
+    C3 li = c3s(0.0f);
+    bool more = false;
+    if (!anyHit) {
+        if (env >= 0) tr = tr * MedTr(S->media[env], ray);
+        li = EvalAllInfinite(S, ray.D);
+    } else {
+        if (env >= 0) {
+            const Ray realPath = mkray(ray.O, ray.D, ray.MinT, Length(At(ray, inct.T)));
+            tr = tr * MedTr(S->media[env], realPath);
+        }
+        if (HasSurface(S, inct)) {
+            if (LightOf(S, inct) >= 0 && LightOf(S, inct) == light) li = IsectLe(S, inct, wle);
+        } else if (++count >= RT_WALK_CAP) {
+            li = EvalAllInfinite(S, ray.D);             /* the walk gives up: a miss */
+        } else {
+            ray = mkray(inct.P, ray.D, 0.001f);
+            env = GetMedium(S, inct, ray.D);
+            more = true;
+        }
+    }
+    if (more) {
+        W.itw_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
+        W.itw_tr[slot] = make_float4(tr.r, tr.g, tr.b, __int_as_float(pack_env(env, count)));
+        itw_push(W, slot, ray);
+        return true;
+    }
+    W.itw_o[slot] = make_float4(li.r, li.g, li.b, 0.0f);
+    W.itw_tr[slot] = make_float4(tr.r, tr.g, tr.b, 0.0f);
+    return false;
+}
+
+/* one shade of a vol_path slot */
+DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting) {
+    const WfJob& J = W.jobs[W.job[slot]];
+    const RtSceneView* S = J.view;
+    const RtParams P = J.P;
+    uint32_t fl = W.flags[slot];
+    /* 1. the boundary walks of a pending direct term */
+    if (fl & (F_WTR | F_WIT)) {
+        if ((fl & F_WTR) && !trw_step(S, W, slot)) fl &= ~F_WTR;
+        if (fl & F_WIT) {
+            const float4 mi = W.pd_mis[slot], wl = W.pd_w[slot];
+            if (!itw_step(S, W, slot, __float_as_int(mi.y), v3(wl.x, wl.y, wl.z))) fl &= ~F_WIT;
+        }
+        if (fl & (F_WTR | F_WIT)) {
+            W.flags[slot] = fl;
+            const int a = warp_append(&W.ctr->n_active[next], true);
+            W.active[next][a] = slot;
+            return;
+        }
+    }
+    float4 cf = W.coeff[slot], rdv = W.rad[slot];
+    C3 coeff = c3(cf.x, cf.y, cf.z), radiance = c3(rdv.x, rdv.y, rdv.z);
+    bool ext = false;
+    for (int pass = 0; pass < 2; pass++) {
+        /* 2. the direct term, now that its walks are done (EstimateDirectSurface / Medium) */
+        if (fl & F_PENDING) {
+            const float4 pc = W.pd_coeff[slot];
+            C3 direct = c3s(0.0f);
+            if (!(fl & F_DZERO)) {
+                C3 le = c3s(0.0f);
+                if (fl & F_L1) {
+                    const float4 l1 = W.pd_l1[slot], lr = W.vol_li[slot], t = W.trw_tr[slot];
+                    const C3 lightLi = c3(lr.x, lr.y, lr.z) * c3(t.x, t.y, t.z);
+                    if (!IsBlack(lightLi)) le = le + c3(l1.x, l1.y, l1.z) * lightLi * l1.w / W.pd_mis[slot].z;
+                }
+                if (fl & F_L2) {
+                    const float4 fr2 = W.pd_fr[slot], mi = W.pd_mis[slot], li = W.itw_o[slot], t = W.itw_tr[slot];
+                    const C3 L = c3(li.x, li.y, li.z);
+                    if (!IsBlack(L)) le = le + c3(fr2.x, fr2.y, fr2.z) * L * c3(t.x, t.y, t.z) * fr2.w / mi.x;
+                }
+                direct = direct + le / pc.w;
+            }
+            radiance = radiance + c3(pc.x, pc.y, pc.z) * direct;
+            fl &= ~(F_PENDING | F_L1 | F_L2 | F_DZERO);
+        }
+        if (fl & F_DONE) break;
+        if (fl & F_CONT) {                       /* 3. the continuation sampled with the term */
+            fl &= ~F_CONT;
+            const float4 ro = W.ray_o[slot], rd = W.ray_d[slot];
+            const int q = warp_append(&W.ctr->n_closest, true);
+            push_ray(W, q, slot, WF_RAY_EXT, mkray(v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ro.w, rd.w));
+            ext = true;
+            break;
+        }
+        if (pass == 1) break;
+        /* 4. one iteration of the Li loop on the extension hit */
+        int2 bc = W.bounce[slot];
+        int bounces = bc.x, guard = bc.y;
+        float4 ro = W.ray_o[slot], rd = W.ray_d[slot];
+        Ray ray = mkray(v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ro.w, rd.w);
+        int env = W.vol_env[slot];
+        const int4 px = W.pix[slot];
+        Rng rand;
+        rng_resume(rand, P.seed, (uint32_t)(P.x0 + px.x), (uint32_t)(P.y0 + px.y), (uint32_t)px.w, W.rng_n[slot]);
+        bool isSpecularPath = (fl & F_SPECULAR) != 0;
+        bool done = false, rr = true;
+        do {
+            if (++guard > RT_LOOP_CAP) { atomicOr(status, RT_STATUS_ITER); done = true; break; }
+            const V3 wo = -ray.D;
+            if (ray.MaxT <= ray.MinT) { done = true; break; }
+            Isect it;
+            const bool isHit = load_hit(S, ray, W.ext_hit[slot], W.ext_sub[slot], &it);
+            MedSample msr; msr.sampled = false;
+            if (env >= 0) {
+                const Ray realRay = mkray(ray.O, ray.D, ray.MinT, isHit ? it.T : kFMax);
+                msr = MedSampleDist(S->media[env], realRay, rand);
+                coeff = coeff * msr.Tr;
+            }
+            if (IsBlack(coeff)) { done = true; break; }
+            if (msr.sampled) {
+                if (bounces >= P.max_depth) { done = true; break; }   /* VolumetricPathTracer.cs:55 */
+                const RtMedium& M = S->media[env];
+                int light;
+                const float lightPdf = SampleLight(S, rand, &light);
+                fl |= F_PENDING;
+                W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+                if (lightPdf > 0.0f) {
+                    const LSample ls = LightSampleLi(S, light, msr.P, rand);
+                    if (ls.Pdf > 0.0f && !IsBlack(ls.Li)) {
+                        const float p = MedP(M, msr.Wo, ls.Wi);
+                        if (p != 0.0f) {
+                            fl |= F_L1 | F_WTR;
+                            const float weight = PowerHeuristic(ls.Pdf, p);
+                            W.pd_l1[slot] = make_float4(p, p, p, weight);
+                            W.vol_li[slot] = make_float4(ls.Li.r, ls.Li.g, ls.Li.b, 0.0f);
+                            const V3 dir = Normalize(ls.P - msr.P);
+                            W.trw_start[slot] = make_float4(msr.P.x, msr.P.y, msr.P.z, __int_as_float(env));
+                            W.trw_end[slot] = make_float4(ls.P.x, ls.P.y, ls.P.z, __int_as_float(0));
+                            W.trw_dir[slot] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                            W.trw_tr[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                        }
+                    }
+                    V3 swi;
+                    const float sp = MedSampleWi(M, msr.Wo, rand, &swi);
+                    if (sp > 0) {
+                        const float b2l = LightPdfLi(S, light, msr.P, swi);
+                        if (b2l != 0.0f) {
+                            fl |= F_L2 | F_WIT;
+                            const float weight = PowerHeuristic(sp, b2l);
+                            const Ray toLight = mkray(msr.P, swi);
+                            W.pd_fr[slot] = make_float4(sp, sp, sp, weight);
+                            W.pd_mis[slot] = make_float4(sp, __int_as_float(light), ls.Pdf, 0.0f);
+                            W.pd_w[slot] = make_float4(-swi.x, -swi.y, -swi.z, 0.0f);
+                            W.itw_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
+                            W.itw_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, 0.0f);
+                            W.itw_tr[slot] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pack_env(env, 0)));
+                        } else {
+                            W.pd_mis[slot] = make_float4(sp, __int_as_float(light), ls.Pdf, 0.0f);
+                        }
+                    } else {
+                        W.pd_mis[slot] = make_float4(0.0f, __int_as_float(light), ls.Pdf, 0.0f);
+                    }
+                } else {
+                    fl |= F_DZERO;
+                }
+                V3 swi;
+                MedSampleWi(M, wo, rand, &swi);
+                ray = mkray(msr.P, swi, ray.MinT);
+                isSpecularPath = false;
+            } else {
+                if (bounces == 0 || isSpecularPath) {
+                    if (isHit) radiance = radiance + coeff * IsectLe(S, it, wo);
+                    else radiance = radiance + coeff * EvalAllInfinite(S, ray.D);
+                }
+                if (!isHit) { done = true; break; }
+                if (P.max_depth != -1 && bounces >= P.max_depth) { done = true; break; }
+                if (!HasSurface(S, it)) {
+                    ray = mkray(it.P, ray.D, ray.MinT);
+                    env = GetMedium(S, it, ray.D);
+                    bounces--;
+                    rr = false;                  /* `continue`: no Russian roulette this iteration */
+                    break;
+                }
+                const int mat = PrimOf(S, it).material;
+                int light;
+                const float lightPdf = SampleLight(S, rand, &light);
+                fl |= F_PENDING;
+                W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+                if (lightPdf > 0.0f) {
+                    const V3 wod = it.Wr;
+                    const LSample ls = LightSampleLi(S, light, it.P, rand);
+                    if (ls.Pdf > 0.0f && !IsBlack(ls.Li)) {
+                        C3 fr = MatFr(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                        const float scatteringPdf = MatPdf(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                        if (!IsBlack(fr)) {
+                            fl |= F_L1 | F_WTR;
+                            fr = fr * AbsCosTheta(Lo(it, ls.Wi));
+                            const float weight = PowerHeuristic(ls.Pdf, scatteringPdf);
+                            W.pd_l1[slot] = make_float4(fr.r, fr.g, fr.b, weight);
+                            W.vol_li[slot] = make_float4(ls.Li.r, ls.Li.g, ls.Li.b, 0.0f);
+                            const V3 dir = Normalize(ls.P - it.P);
+                            W.trw_start[slot] = make_float4(it.P.x, it.P.y, it.P.z, __int_as_float(env));
+                            W.trw_end[slot] = make_float4(ls.P.x, ls.P.y, ls.P.z, __int_as_float(0));
+                            W.trw_dir[slot] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                            W.trw_tr[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+                        }
+                    }
+                    const BSample sample = MatSample(S, mat, Lo(it, wod), it.UV, rand);
+                    const C3 fr = sample.Fr * AbsCosTheta(sample.Wi);
+                    const float scatteringPdf = sample.Pdf;
+                    const bool sampledSpecular = (sample.Type & BX_SPECULAR) != 0;
+                    float mis_pdf = 0.0f;
+                    if (!IsBlack(fr) && scatteringPdf > 0) {
+                        float weight = 1;
+                        bool go = true;
+                        if (!sampledSpecular) {
+                            const float b2l = LightPdfLi(S, light, it.P, Wo(it, sample.Wi));
+                            if (b2l == 0.0f) go = false;
+                            else weight = PowerHeuristic(scatteringPdf, b2l);
+                        }
+                        if (go) {
+                            fl |= F_L2 | F_WIT;
+                            mis_pdf = scatteringPdf;
+                            const Ray toLight = Spawn(it, Wo(it, sample.Wi));
+                            const V3 wle = Wo(it, -sample.Wi);
+                            W.pd_fr[slot] = make_float4(fr.r, fr.g, fr.b, weight);
+                            W.pd_w[slot] = make_float4(wle.x, wle.y, wle.z, 0.0f);
+                            W.itw_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
+                            W.itw_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, 0.0f);
+                            W.itw_tr[slot] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pack_env(env, 0)));
+                        }
+                    }
+                    W.pd_mis[slot] = make_float4(mis_pdf, __int_as_float(light), ls.Pdf, 0.0f);
+                } else {
+                    fl |= F_DZERO;
+                }
+                const BSample sample = MatSample(S, mat, Lo(it, wo), it.UV, rand);
+                isSpecularPath = (sample.Type & BX_SPECULAR) != 0;
+                if (sample.Pdf > 0.0f) coeff = coeff * (sample.Fr * AbsCosTheta(sample.Wi) / sample.Pdf);
+                else { done = true; break; }
+                const V3 nextDir = Wo(it, sample.Wi);
+                ray = mkray(it.P, nextDir, ray.MinT);
+                env = GetMedium(S, it, nextDir);
+            }
+        } while (false);
+        if (!done && rr && bounces > P.min_depth) {
+            const float q = nmin(MaxElement(coeff), P.rr);
+            if (NextFloat(rand) > q) done = true;
+            else coeff = coeff / q;
+        }
+        if (!done) {
+            bounces++;
+            fl |= F_CONT;
+            W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
+            W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
+            W.vol_env[slot] = env;
+        } else {
+            fl |= F_DONE;
+        }
+        W.bounce[slot] = make_int2(bounces, guard);
+        W.rng_n[slot] = rand.n;
+        fl = (fl & ~F_SPECULAR) | (isSpecularPath ? F_SPECULAR : 0u);
+        /* start the walks of the new direct term; if there are none, resolve it now */
+        if (fl & F_WTR) {
+            if (!trw_push(W, slot)) fl &= ~F_WTR;
+        }
+        if (fl & F_WIT) {
+            const float4 o = W.itw_o[slot], d = W.itw_d[slot];
+            itw_push(W, slot, mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w));
+        }
+        if (fl & (F_WTR | F_WIT)) break;
+    }
+    W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.0f);
+    W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
+    if (ext || (fl & (F_WTR | F_WIT))) {
+        W.flags[slot] = fl;
+        const int a = warp_append(&W.ctr->n_active[next], true);
+        W.active[next][a] = slot;
+        return;
+    }
+    /* the path is over */
+    finish_path(J, W, slot, radiance, stats, WF_PASS_RENDER);
+    if (counting) warp_add64(stats + 0, 1u);
+    if (start_path(W, slot, true)) {
+        const int a = warp_append(&W.ctr->n_active[next], true);
+        W.active[next][a] = slot;
+    } else {
+        W.flags[slot] = 0;
+        warp_append(&W.ctr->n_active[next], false);
+    }
+}
+
+__global__ void __launch_bounds__(128, 4) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
+                                                         bool counting) {
+    const int cur = W.ctr->iter & 1;
+    const int n = min(W.ctr->n_active[cur], W.slots);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) shade_vol_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+}
+
 /* the active paths of this iteration, one thread each over the sorted list:
  * either a grid sized to the active count, or (kDynamic, inside a graph where
  * the count is unknown at launch) a resident grid whose warps take the next
@@ -613,7 +979,9 @@ __global__ void k_wf_active_init(WfState W) {
  * 0 finished (pending term, then a new sample), 1 missed the scene, 2 hit a
  * medium boundary without a surface, 3 + RT_MAT_* hit that material type. */
 DF int shade_key(const WfState& W, int slot) {
-    if (W.flags[slot] & F_DONE) return 0;
+    const uint32_t fl = W.flags[slot];
+    if (fl & (F_WTR | F_WIT)) return WF_SHADE_KEYS - 1;     /* vol_path: advancing boundary walks */
+    if (fl & F_DONE) return 0;
     const int hs = __float_as_int(W.ext_hit[slot].w);
     if (hs < 0) return 1;
     const RtSceneView* S = W.jobs[W.job[slot]].view;
@@ -723,7 +1091,7 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
 
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
                         cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
-                        int pass, const WfAdjoint* adj) {
+                        int pass, const WfAdjoint* adj, bool vol) {
     static const int sort_blocks = resident_blocks(k_wf_sort_scatter, 256);
     static const int shade_blocks = resident_blocks(k_wf_shade<false, true>, 128);
     const WfAdjoint A = adj ? *adj : WfAdjoint{-1, 0, nullptr, nullptr, nullptr, nullptr};
@@ -734,7 +1102,8 @@ cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned
         const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
         k_wf_sort_count<<<sb, 256, 0, s>>>(W);
         k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
-        if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A);
+        if (vol) k_wf_shade_vol<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
+        else if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A);
         else if (pass == WF_PASS_REPLAY) k_wf_shade<true, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
         else k_wf_shade<false, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
         *launches += 3;

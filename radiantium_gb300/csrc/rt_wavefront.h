@@ -16,7 +16,9 @@
 #include <stdint.h>
 #include "rt_types.h"
 
-enum { WF_RAY_EXT = 0, WF_RAY_SHADOW = 1, WF_RAY_MIS = 2 };
+/* ray kinds: extension, shadow (any hit), MIS / IntersectTr-walk segment,
+ * Transmittance-walk segment (the last three closest hit except shadow) */
+enum { WF_RAY_EXT = 0, WF_RAY_SHADOW = 1, WF_RAY_MIS = 2, WF_RAY_TRW = 3 };
 
 #define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
 #define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
@@ -96,6 +98,16 @@ struct WfState {
     /* adjoint replay: d ln (f w) / d alpha of the pending light and BSDF terms,
      * d ln f / d alpha of the continuation, alpha slot of the pending vertex */
     float4* adj_rho;
+    /* vol_path: the ray's medium, and the two boundary walks of a pending
+     * direct term - Scene.Transmittance towards the light sample (start +
+     * medium, end + segment count, direction, throughput) and
+     * Scene.IntersectTr along the phase / BSDF sample (ray + medium, throughput
+     * + segment count) - with the raw light-sample radiance */
+    int32_t* vol_env;
+    float4* trw_start; float4* trw_end; float4* trw_dir; float4* trw_tr;
+    float4* itw_o; float4* itw_d; float4* itw_tr;
+    float4* vol_li;
+    float4* trw_hit; int32_t* trw_sub;
 };
 
 /* Starts the round: every slot takes a camera sample, the first active list
@@ -110,6 +122,6 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
  * Kernel launches are added to *launches. */
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
                         cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
-                        int pass = WF_PASS_RENDER, const WfAdjoint* adj = nullptr);
+                        int pass = WF_PASS_RENDER, const WfAdjoint* adj = nullptr, bool vol = false);
 
 #endif

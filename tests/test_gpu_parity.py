@@ -165,14 +165,36 @@ def test_wavefront_matches_megakernel_large(dev):
     assert np.array_equal(_bits(b[20:44, 30:46]), _bits(o))
 
 
-def test_render_volume_bitexact(dev):
+@pytest.mark.parametrize("renderer", RENDERERS)
+def test_render_volume_bitexact(dev, renderer):
+    """vol_path: the megakernel for both light strategies, the wavefront (with its
+    boundary walks traced as queued segments) for the Uniform strategy."""
     s, st = procedural.volume_box(40, 40)
     orc = OracleScene(s)
     dev.upload(s)
     for strategy in (N.STRATEGY_UNIFORM, N.STRATEGY_ALL):
+        if renderer != N.RENDERER_MEGAKERNEL and strategy == N.STRATEGY_ALL:
+            continue
         stx = st.replace(strategy=strategy)
-        g, o = dev.render(stx), orc.render(stx)
+        g, o = _render(dev, stx, renderer), orc.render(stx)
         assert np.array_equal(_bits(g), _bits(o)), f"max abs diff {np.abs(g - o).max()}"
+
+
+def test_volume_wavefront_matches_megakernel_large(dev):
+    """vol_path on the C3 geometry at reduced size: wavefront == megakernel, with
+    several rounds and heavy slot reuse, and the counters of both agree."""
+    s, st = procedural.volume_sphere(64, 64, sphere_n=24)
+    dev.upload(s)
+    stx = st.replace(spp=8, max_depth=12)
+    dev.set_counting(True)
+    a = _render(dev, stx, N.RENDERER_MEGAKERNEL)
+    ca = dev.stats()
+    b = _render(dev, stx, N.RENDERER_WAVEFRONT)
+    cb = dev.stats()
+    dev.set_counting(False)
+    assert np.array_equal(_bits(a), _bits(b)), f"max abs diff {np.abs(a - b).max()}"
+    for k in ("samples", "rays_closest", "node_visits", "prim_tests"):
+        assert ca[k] == cb[k], (k, ca[k], cb[k])
 
 
 def test_render_crop_and_resume(dev, cornell):
