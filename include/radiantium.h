@@ -359,8 +359,9 @@ typedef struct rt_batch_item {
  * path slots and every trace / shade launch, so small scenes do not leave
  * the GPU idle and the launch overhead is paid once per bounce for the whole
  * batch.  Each film equals what rt_render gives for the same item, bit for
- * bit.  Every item must use the `path` integrator with the Uniform light
- * strategy, and all scene contexts must be on the batch context's device.
+ * bit.  All items must use the same integrator (`path` or `vol_path`) with
+ * the Uniform light strategy, and all scene contexts must be on the batch
+ * context's device.
  * The bounce loop is driven from the host, or runs as a CUDA graph when
  * rt_set_renderer selected RT_RENDERER_WAVEFRONT_GRAPH.  No counterpart in
  * the reference, which renders one scene per process

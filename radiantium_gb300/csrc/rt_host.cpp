@@ -978,8 +978,9 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
         if (sc->device != c->device) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " is on another device");
         if (!sc->has_scene) throw RtFail(RT_ERR_NO_SCENE, "render_batch: item " + std::to_string(i) + " has no uploaded scene");
         if (p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " has spp <= 0");
-        if (p->integrator != RT_INTEGRATOR_PATH || p->strategy != RT_STRATEGY_UNIFORM)
-            throw RtFail(RT_ERR_UNSUPPORTED, "render_batch: items must use the path integrator with the Uniform light strategy");
+        if ((p->integrator != RT_INTEGRATOR_PATH && p->integrator != RT_INTEGRATOR_VOL_PATH) ||
+            p->strategy != RT_STRATEGY_UNIFORM || p->integrator != items[0].params.integrator)
+            throw RtFail(RT_ERR_UNSUPPORTED, "render_batch: items must share the path or vol_path integrator and use the Uniform light strategy");
         RtParams P{};
         P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
         P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;

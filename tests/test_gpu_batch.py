@@ -108,12 +108,39 @@ def test_batch_repeats_and_single_graph_render(scenes):
     assert np.array_equal(_bits(g), _bits(w))
 
 
+def test_batch_of_volumes_matches_single_renders():
+    vols = [procedural.volume_box(40, 40, seed=s) for s in (9, 10)]
+    devs = []
+    try:
+        for s, st in vols:
+            d = Device(0)
+            d.upload(s)
+            devs.append((d, st))
+        items = [(devs[0][0], devs[0][1].replace(spp=3, seed=2)), (devs[1][0], devs[1][1].replace(spp=5, seed=3)),
+                 (devs[0][0], devs[0][1].replace(spp=2, seed=4, x0=5, y0=7, width=20, height=16))]
+        want = _singles(items)
+        host = Device(0)
+        try:
+            _set_limits(host, 2500, 256)
+            got = host.render_batch(items)
+            for g, w in zip(got, want):
+                assert np.array_equal(_bits(g), _bits(w))
+        finally:
+            host.close()
+    finally:
+        for d, _ in devs:
+            d.close()
+
+
 def test_batch_rejects_unsupported_items(scenes):
-    (a, sa), _, _ = scenes
+    (a, sa), (b, sb), _ = scenes
     host = Device(0)
     try:
         with pytest.raises(N.RTError) as e:
-            host.render_batch([(a, sa.replace(spp=1, integrator=N.INTEGRATOR_VOL_PATH))])
+            host.render_batch([(a, sa.replace(spp=1)), (b, sb.replace(spp=1, integrator=N.INTEGRATOR_VOL_PATH))])
+        assert e.value.code == N.RT_ERR_UNSUPPORTED
+        with pytest.raises(N.RTError) as e:
+            host.render_batch([(a, sa.replace(spp=1, strategy=N.STRATEGY_ALL))])
         assert e.value.code == N.RT_ERR_UNSUPPORTED
         with pytest.raises(N.RTError) as e:
             host.render_batch([(a, sa.replace(spp=1))] * (N.MAX_BATCH + 1))
