@@ -376,6 +376,9 @@ struct Best {
 };
 
 #define RT_TRAVERSAL_CAP (1u << 26)   /* loop steps of one two-level traversal */
+#ifndef RT_DESCEND
+#define RT_DESCEND 2                   /* interior nodes one traversal step may visit */
+#endif
 #define RT_NO_NODE ((int)0x80000000)
 
 /* Leaf primitive of either level against ray r: triangle or sphere (the
@@ -544,16 +547,19 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t*
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        if (T.sp - T.base == RT_STACK_SIZE) {
-            atomicOr(status, RT_STATUS_STACK);
-            if (!T.inProto) return true;
-            T.sp = T.base;                      /* the prototype's traversal stops here */
-            T.cur = RT_NO_NODE;
-            return false;
+        /* up to RT_DESCEND interior nodes (with the pops that follow them) per step */
+        for (int k = 0; k < RT_DESCEND && T.cur >= 0; k++) {
+            if (T.sp - T.base == RT_STACK_SIZE) {
+                atomicOr(status, RT_STATUS_STACK);
+                if (!T.inProto) return true;
+                T.sp = T.base;                  /* the prototype's traversal stops here */
+                T.cur = RT_NO_NODE;
+                return false;
+            }
+            if (st) st->nodes++;
+            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         }
-        if (st) st->nodes++;
-        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
-        if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
@@ -671,16 +677,18 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status,
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        if (T.sp - T.base == RT_STACK_SIZE) {
-            atomicOr(status, RT_STATUS_STACK);
-            if (!T.inProto) return true;
-            T.sp = T.base;
-            T.cur = RT_NO_NODE;
-            return false;
+        for (int k = 0; k < RT_DESCEND && T.cur >= 0; k++) {
+            if (T.sp - T.base == RT_STACK_SIZE) {
+                atomicOr(status, RT_STATUS_STACK);
+                if (!T.inProto) return true;
+                T.sp = T.base;
+                T.cur = RT_NO_NODE;
+                return false;
+            }
+            if (st) st->nodes++;
+            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         }
-        if (st) st->nodes++;
-        T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
-        if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
