@@ -5,6 +5,8 @@ Translation units compiled in parallel and linked with nvcc:
                  multiply and add separately rounded (the reference's
                  arithmetic), IEEE division and square root are nvcc's
                  defaults;
+  rt_bvh_gpu.cu  the reference's SAH tree built on the GPU (--fmad=false:
+                 bucket costs round like the host builder's);
   rt_noalloc.cu  the fixed scratch array of the allocation-free render;
   rt_host.cpp, rt_bvh.cpp  host runtime and BVH builder, -ffp-contract=off
                  for the same reason.
@@ -44,6 +46,8 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
                             "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_wavefront.cu")],
         "rt_adjoint.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_adjoint.cu")],
+        "rt_bvh_gpu.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                         *extra_nvcc, "-c", os.path.join(CSRC, "rt_bvh_gpu.cu")],
         "rt_noalloc.o": [nvcc, ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *extra_nvcc,
                          "-c", os.path.join(CSRC, "rt_noalloc.cu")],
         "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",

@@ -29,6 +29,7 @@
 #include "../../include/radiantium.h"
 #include "../../include/rt_detmath.h"
 #include "rt_bvh.h"
+#include "rt_bvh_gpu.h"
 #include "rt_launch.h"
 #include "rt_types.h"
 #include "rt_wavefront.h"
@@ -94,6 +95,7 @@ struct Ctx {
     int wf_capacity = WF_MAX_SLOTS;            /* path slots in flight */
     int wf_refill = 8;                         /* idle lanes before a trace warp fetches (1..32) */
     bool wf_graph_pref = false;                /* RT_RENDERER_AUTO drives the wavefront as a graph */
+    int gpu_build_min = 1 << 15;               /* trees of at least this many primitives build on the GPU */
     uint64_t wf_generation = 0;                /* bumped whenever the path-state buffers move */
     /* the bounce loop captured as a CUDA graph while-loop */
     cudaGraph_t wf_graph = nullptr;
@@ -266,6 +268,17 @@ void check_index(int i, int n, const char* what) {
 }
 
 /* builds one BVH; appends nodes and slots; fills the header */
+/* The reference's SAH tree: on the GPU for large primitive counts (the same
+ * tree, rt_bvh_gpu.cu), on the host threads otherwise. */
+rtb::BuildResult build_tree(Ctx* c, const std::vector<rtb::Box>& boxes, int maxp, int threads) {
+    if ((int64_t)boxes.size() >= c->gpu_build_min) {
+        rtb::BuildResult r;
+        CK(rt_gpu_build_sah(boxes, maxp, &r, c->stream));
+        return r;
+    }
+    return rtb::build_sah(boxes, maxp, threads);
+}
+
 void emit_bvh(const rtb::BuildResult& br, const std::vector<std::array<float4, 3>>& recs, std::vector<float4>& nodes,
               std::vector<float4>& slots, RtBvh* hdr) {
     const int slot_base = (int)(slots.size() / 3);
@@ -427,7 +440,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
                 throw RtFail(RT_ERR_INVALID_ARG, "scene: instanced prototype groups must be meshes or spheres");
             }
         }
-        rtb::BuildResult br = rtb::build_sah(boxes, maxp, threads);
+        rtb::BuildResult br = build_tree(c, boxes, maxp, threads);
         tallest = std::max(tallest, br.max_depth);
         emit_bvh(br, recs, nodes, slots, &bvhs[1 + b]);
         if (!br.nodes.empty()) blas_root[b] = br.nodes[0].bounds;
@@ -512,7 +525,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
         }
     }
     if (prims.empty()) throw RtFail(RT_ERR_INVALID_ARG, "scene: no primitives");
-    rtb::BuildResult top = rtb::build_sah(boxes, maxp, threads);
+    rtb::BuildResult top = build_tree(c, boxes, maxp, threads);
     tallest = std::max(tallest, top.max_depth);
     emit_bvh(top, recs, nodes, slots, &bvhs[0]);
 
@@ -1390,6 +1403,36 @@ int rt_debug_bvh(const float* boxes, int n, int max_prims, int64_t* node_count, 
     } catch (...) {
         return RT_ERR_OOM;
     }
+}
+
+/* test hook (not part of radiantium.h): the GPU builder's tree in rt_debug_bvh's layout */
+int rt_debug_bvh_gpu(void* ctx, const float* boxes, int n, int max_prims, int64_t* node_count, float* bounds,
+                     int32_t* idx, int32_t* count, int32_t* axis, int32_t* order, int32_t* depth) {
+    Ctx* c = (Ctx*)ctx;
+    if (!boxes || n <= 0 || !node_count) return RT_ERR_INVALID_ARG;
+    return run(c, [&]() {
+        std::vector<rtb::Box> b(n);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) { b[i].mn[k] = boxes[6 * i + k]; b[i].mx[k] = boxes[6 * i + 3 + k]; }
+        rtb::BuildResult r;
+        CK(rt_gpu_build_sah(b, max_prims, &r, c->stream));
+        *node_count = (int64_t)r.nodes.size();
+        if (depth) *depth = r.max_depth;
+        if (bounds) {
+            for (size_t i = 0; i < r.nodes.size(); i++) {
+                for (int k = 0; k < 3; k++) { bounds[6 * i + k] = r.nodes[i].bounds.mn[k]; bounds[6 * i + 3 + k] = r.nodes[i].bounds.mx[k]; }
+                idx[i] = r.nodes[i].second; count[i] = r.nodes[i].count; axis[i] = r.nodes[i].axis;
+            }
+            for (int i = 0; i < n; i++) order[i] = r.order[i];
+        }
+    });
+}
+/* test hook: primitive count from which upload_scene builds trees on the GPU */
+int rt_debug_set_gpu_build(void* ctx, int min_prims) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || min_prims < 0) return RT_ERR_INVALID_ARG;
+    c->gpu_build_min = min_prims == 0 ? INT_MAX : min_prims;
+    return RT_OK;
 }
 
 /* test hook (not part of radiantium.h): runs rt_detmath (fn 0..7) or CUDA's
