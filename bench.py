@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["instanced", "cornell", "volume", "batch", "adjoint"], default="instanced")
+    ap.add_argument("--workload", choices=["instanced", "cornell", "volume", "batch", "adjoint", "particle"],
+                    default="instanced")
+    ap.add_argument("--particles-per-step", type=int, default=1 << 24, help="particle workload: particles per step")
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -779,8 +781,190 @@ def run_adjoint(args):
     return 0
 
 
+def particle_workload():
+    """The light tracer's workload: the reference's own particle example shape
+    (Example/cbox/test_adjoint_particle.json: Cornell box, 800x600, min_depth 7,
+    unbounded depth with Russian roulette 0.99), on the procedural Cornell box."""
+    from radiantium_gb300 import native as N, procedural
+    scene, st = procedural.cornell_box(800, 600)
+    return scene, st.replace(integrator=N.INTEGRATOR_PARTICLE, max_depth=-1, min_depth=7, rr_threshold=0.99, seed=1)
+
+
+def particle_config(scene, st, per_step):
+    return {"workload": "adjoint_particle light tracer, procedural Cornell box (36 tris, ceiling quad light), "
+                        "min_depth 7, unbounded depth, RR 0.99 (shape of Example/cbox/test_adjoint_particle.json)",
+            "film": [scene.camera.width, scene.camera.height], "particles_per_step": per_step,
+            "max_depth": st.max_depth, "min_depth": st.min_depth, "integrator": "adjoint_particle",
+            "triangles": scene.triangle_count, "seed": st.seed}
+
+
+def particle_cpu(scene, st, target_s, cores):
+    """particles/s of the oracle's light tracer on all host cores, bounded to about target_s."""
+    from oracle.oracle import OracleScene
+    orc = OracleScene(scene)
+    t0 = time.perf_counter()
+    orc.render_particles(st, 20000, threads=cores)
+    t1 = time.perf_counter() - t0
+    n = int(max(20000, min(1 << 26, 20000 * target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    orc.render_particles(st, n, first=20000, threads=cores)
+    dt = time.perf_counter() - t0
+    orc.close()
+    return n, dt
+
+
+def run_particle_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    scene, st = particle_workload()
+    cores = os.cpu_count() or 1
+    from oracle.oracle import OracleScene
+    orc = OracleScene(scene)
+    t0 = time.perf_counter()
+    orc.render_particles(st, 20000, threads=cores)
+    t1 = time.perf_counter() - t0
+    total_steps = args.steps + args.warmup
+    n = int(max(20000, 20000 * (150.0 / total_steps) / max(t1, 1e-3)))
+    for i in range(args.warmup):
+        orc.render_particles(st, n, first=i * n, threads=cores)
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        orc.render_particles(st, n, first=(args.warmup + i) * n, threads=cores)
+        times.append(time.perf_counter() - t0)
+    orc.close()
+    ms = 1000.0 * float(np.mean(times))
+    value = n / (ms / 1000.0)
+    desc = f"{n} particles per step over the whole film (scale + CameraTraceLight included)"
+    print(json.dumps({
+        "impl": "reference", "metric": "particles/s (adjoint_particle light tracer)", "value": value,
+        "unit": "particles/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)", "config": dict(particle_config(scene, st, n), step=desc),
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
+                         "sample": desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
+                                          "(oracle/) runs on all host cores"},
+        "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+        flush=True)
+    return 0
+
+
+def run_particles(args):
+    """The light tracer: one step = --particles-per-step particles splatted into the
+    whole film, then the film scale and CameraTraceLight pass."""
+    import torch
+    from radiantium_gb300.device import Device
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    scene, st = particle_workload()
+    dev = Device(local)
+    dev.upload(scene)
+    W, H = scene.camera.width, scene.camera.height
+    per = args.particles_per_step
+    base = rank * (args.warmup + 2 * args.steps + 1) * per    # disjoint particle ranges per rank
+    film = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    dev.set_counting(True)
+    dev.render_particles_device(st, per, film.data_ptr(), first=base, stream=stream)
+    torch.cuda.synchronize()
+    counts = dev.stats()
+    dev.set_counting(False)
+    for i in range(args.warmup):
+        dev.render_particles_device(st, per, film.data_ptr(), first=base + (1 + i) * per, stream=stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, kernel_ms, launches = [], 0.0, 0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dev.render_particles_device(st, per, film.data_ptr(), first=base + (1 + args.warmup + i) * per, stream=stream)
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        s = dev.stats()
+        kernel_ms += s["render_kernel_ms"]
+        launches += s["kernel_launches"]
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = per * world / (ms_step / 1000.0)
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        host = torch.empty(W * H * 3, dtype=torch.float32, pin_memory=True).numpy()
+        p = host.ctypes.data_as(C.c_void_p)
+        prm = st.to_c()
+        times = []
+        for i in range(args.steps):
+            t0 = time.perf_counter()
+            rc = dev.lib.rt_render_particles(dev.h, C.byref(prm), base + (1 + args.warmup + args.steps + i) * per,
+                                             per, p)
+            times.append(time.perf_counter() - t0)
+            if rc != 0:
+                raise RuntimeError(dev.lib.rt_last_error(dev.h).decode())
+        e2e = {"value": per * world / float(np.mean(times)), "unit": "particles/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": W * H * 12, "note": "rt_render_particles with a pinned host film"}
+    # roofline of k_particles: algorithmic bytes from exact counts (the finishing
+    # pass's W*H camera rays are in the counts too; the splats' film atomics are not)
+    alg = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
+           + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"])
+    kms = kernel_ms / args.steps
+    achieved = alg / (kms / 1000.0) / 1e9
+    peak, peak_src = measured_peak()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        n, dt = particle_cpu(scene, st, args.cpu_seconds, cores)
+        cpu = {"value": n / dt, "unit": "particles/s", "cores": cores, "kind": "port",
+               "sample": f"{n} particles of the same workload over the whole film ({dt:.1f} s)"}
+    line = {
+        "metric": "particles/s (adjoint_particle light tracer)", "value": value, "unit": "particles/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)",
+        "config": dict(particle_config(scene, st, per), parallelism=f"replicas x{world} (disjoint particle ranges)",
+                       l2="256 MiB flush between timed steps (outside the CUDA events)",
+                       renderer="k_particles (one thread per particle) + k_particle_finish"),
+        "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src, "kernel": "k_particles",
+                     "alg_bytes_per_step": alg, "kernel_ms_per_step": kms},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
+                                                   "prim_tests", "instance_visits")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dev.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "particle":
+        return run_particle_reference(args) if args.impl == "reference" else run_particles(args)
     if args.workload == "adjoint":
         if args.impl == "reference":
             return run_reference(args)

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define RT_ABI_VERSION 1
+#define RT_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------- */
 #define RT_OK 0
@@ -71,6 +71,7 @@ extern "C" {
 
 #define RT_INTEGRATOR_PATH 0      /* Integrators/PathTracer.cs */
 #define RT_INTEGRATOR_VOL_PATH 1  /* Integrators/VolumetricPathTracer.cs */
+#define RT_INTEGRATOR_PARTICLE 2  /* Integrators/AdjointParticleIntegrator.cs ("adjoint_particle") */
 #define RT_METHOD_BXDF 0          /* PathTracer.cs:12-17 PathSampleMethod */
 #define RT_METHOD_NEE 1
 #define RT_METHOD_MIS 2
@@ -151,13 +152,18 @@ typedef struct rt_group_desc {
     float world_to_model[16]; /* INSTANCE, INFINITE_LIGHT (Matrix4x4.Invert of the above) */
 } rt_group_desc;
 
-/* PerspectiveCamera (Camera.cs:79-191); the matrices are the ones Update()
- * derives (clip->camera is the inverse of perspective*translate*scale). */
+/* PerspectiveCamera (Camera.cs:81-241); the matrices are the ones Update()
+ * derives (Camera.cs:128-180): camera->clip is perspective*translate*scale,
+ * clip->camera its Matrix4x4.Invert, world->camera the Invert of
+ * camera->world.  The light tracer (SampleWi, Camera.cs:221-241) reads the
+ * camera->clip and world->camera matrices; the camera rays read the other two. */
 typedef struct rt_camera_desc {
     int32_t width, height;    /* ScreenX, ScreenY */
     float near_z, far_z;
     float clip_to_camera[16];
     float camera_to_world[16];
+    float camera_to_clip[16];
+    float world_to_camera[16];
 } rt_camera_desc;
 
 typedef struct rt_scene_desc {
@@ -371,6 +377,39 @@ int rt_render_batch(void* ctx, const rt_batch_item* items, int n);
 /* Same, every out_rgb a device pointer written on `stream` (NULL = the
  * context stream); returns once the films are written. */
 int rt_render_batch_device(void* ctx, const rt_batch_item* items, int n, void* stream);
+
+/* ---- light tracing ----------------------------------------------------------
+ * The "adjoint_particle" renderer + integrator (Renderers/AdjointParticleRenderer.cs,
+ * Integrators/AdjointParticleIntegrator.cs): particles leave the lights
+ * (Light.SampleEmit), and every surface vertex is connected to the camera
+ * (PerspectiveCamera.SampleWi) and splatted into the film when visible.  The
+ * film is then scaled by ScreenX * ScreenY / particle_count
+ * (AdjointParticleRenderer.cs:156-164) and each pixel (x, y) gains
+ * CameraTraceLight of the camera ray through screen position (x, y)
+ * (AdjointParticleRenderer.cs:166-172).
+ *
+ * Particle i (0 <= i < 2^63) draws its random numbers from the Philox
+ * stream with counter (i mod 2^32, i / 2^32, RT_PARTICLE_STREAM) and key
+ * params->seed, so a range of particles renders the same on any number of
+ * calls or devices; films of disjoint ranges combine as their
+ * particle-count-weighted mean.  Splats are added with float atomics, so the
+ * film's low bits depend on their order (as under the reference's lock).
+ * A splat whose screen position is NaN (the reference's ColorBuffer throws
+ * there) is dropped. */
+#define RT_PARTICLE_STREAM 0x80000000u
+
+/* Traces particles [first_particle, first_particle + particle_count) and
+ * writes the whole film (ScreenX * ScreenY * 3 floats, ColorBuffer layout) to
+ * host memory.  params: integrator RT_INTEGRATOR_PARTICLE, max_depth,
+ * min_depth, rr_threshold ("max_depth", "min_depth", "rr_threshold",
+ * RendererBuilder.cs:73-79), seed; the crop fields must be 0 (whole film).
+ * particle_count >= 1 ("particle_count", RendererBuilder.cs:36-41). */
+int rt_render_particles(void* ctx, const rt_render_params* params, int64_t first_particle,
+                        int64_t particle_count, float* out_rgb);
+
+/* Same, film written to device memory on `stream` (NULL = the context stream). */
+int rt_render_particles_device(void* ctx, const rt_render_params* params, int64_t first_particle,
+                               int64_t particle_count, float* d_out_rgb, void* stream);
 
 /* Settings chosen by rt_autotune. */
 typedef struct rt_tune_result {

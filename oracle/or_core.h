@@ -143,6 +143,7 @@ static inline C3 operator/(float s, C3 a) { return c3(s / a.r, s / a.g, s / a.b)
 static inline bool operator==(C3 a, C3 b) { return a.r == b.r && a.g == b.g && a.b == b.b; }
 static inline bool operator!=(C3 a, C3 b) { return !(a == b); }
 static inline bool IsBlack(C3 a) { return a == c3s(0.0f); }
+static inline float Floor(float x) { return std::floor(x); }
 static inline bool IsValid(C3 c) {
     if (c.r < 0 || isinf_(c.r) || isnan_(c.r)) return false;
     if (c.g < 0 || isinf_(c.g) || isnan_(c.g)) return false;
@@ -342,6 +343,24 @@ static inline V3 SquareToUniformSphere(V2 s) {
     float sinPhi = Sin(phi), cosPhi = Cos(phi);
     return v3(sinTheta * cosPhi, sinTheta * sinPhi, cosTheta);
 }
+
+/* Probability.SquareToConcentricDisk (Probability.cs:157-174), Shirley-Chiu mapping */
+static inline V2 SquareToConcentricDisk(V2 u) {
+    V2 uOffset = v2(2.0f * u.x - 1.0f, 2.0f * u.y - 1.0f);
+    if (uOffset.x == 0 && uOffset.y == 0) return v2(0, 0);
+    float theta, r;
+    if (Abs(uOffset.x) > Abs(uOffset.y)) {
+        r = uOffset.x;
+        theta = (kPI / 4) * (uOffset.y / uOffset.x);
+    } else {
+        r = uOffset.y;
+        theta = (kPI / 2) - (kPI / 4) * (uOffset.x / uOffset.y);
+    }
+    float sinTheta = Sin(theta), cosTheta = Cos(theta);
+    return v2(r * cosTheta, r * sinTheta);
+}
+/* Probability.SquareToCosineHemispherePdf (Probability.cs:102-105) */
+static inline float SquareToCosineHemispherePdf(V3 v) { return v.z / kPI; }
 
 /* PathUtility.PowerHeuristic (computed in double) */
 static inline float PowerHeuristic(int nf, float fPdf, int ng, float gPdf) {

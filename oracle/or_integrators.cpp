@@ -331,6 +331,55 @@ C3 VolPathLi(const Scene& scene, const rt_render_params& P, Ray ray, Rng& rand) 
     return radiance;
 }
 
+/* ---- AdjointParticleIntegrator (Integrators/AdjointParticleIntegrator.cs) ---------------- */
+/* EmitParticle (:24-79): one particle from a light, every surface vertex connected to the camera */
+void EmitParticle(const Scene& scene, const rt_render_params& P, Rng& rand, std::vector<Splat>* splats) {
+    const Light* light = nullptr;
+    float selectPdf = scene.SampleLight(rand, &light);
+    if (selectPdf == 0.0f) return;
+    LightEmitResult emit = light->SampleEmit(rand);
+    if (IsBlack(emit.Radiance)) return;
+    const PerspectiveCamera& camera = scene.Camera;
+    C3 coeff = emit.Radiance * AbsDot(emit.Dir, emit.Normal) / (selectPdf * emit.PdfPos * emit.PdfDir);
+    Ray lightRay(emit.Pos, emit.Dir, 0.0001f);
+    int guard = 0;
+    for (int bounces = 1;; bounces++) {
+        if (++guard > kLoopCap) break;
+        if (P.max_depth != -1 && bounces >= P.max_depth) break;
+        if (bounces > P.min_depth) {
+            if (rand.NextFloat() > P.rr_threshold) break;
+            coeff = coeff / P.rr_threshold;
+        }
+        Intersection inct;
+        if (!scene.Intersect(lightRay, &inct)) break;
+        if (!inct.HasSurface()) {
+            lightRay = Ray(inct.P, lightRay.D, lightRay.MinT);
+            bounces--;
+            continue;
+        }
+        SampleCameraWiResult sample = camera.SampleWi(inct.P);
+        if (sample.Pdf > 0 && !IsBlack(sample.We)) {
+            if (!scene.IsOccluded(sample.Pos, inct.P)) {
+                C3 f = inct.Surface()->Fr(inct.ToLocal(inct.Wr), inct.ToLocal(sample.Dir), inct, true);
+                float absCos = AbsCosTheta(inct.ToLocal(sample.Dir));
+                C3 color = coeff * f * sample.We * absCos / sample.Pdf;
+                V2 ss = sample.ScreenPos;
+                /* the reference's ColorBuffer throws on a NaN position; it is dropped here */
+                if (ss.x == ss.x && ss.y == ss.y) splats->push_back(Splat{(int)Floor(ss.x), (int)Floor(ss.y), color});
+            }
+        }
+        SampleBxdfResult bs = inct.Surface()->Sample(inct.ToLocal(inct.Wr), inct, rand, true);
+        if (bs.Pdf > 0.0f) coeff = coeff * (bs.Fr * AbsCosTheta(bs.Wi) / bs.Pdf);
+        else break;
+        lightRay = inct.SpawnRay(inct.ToWorld(bs.Wi));
+    }
+}
+/* CameraTraceLight (:81-84) */
+C3 CameraTraceLight(const Scene& scene, const Ray& ray) {
+    Intersection inct;
+    return scene.Intersect(ray, &inct) ? inct.Le(-ray.D) : scene.EvalAllInfiniteLights(ray);
+}
+
 /* one camera sample of BlockBasedRenderer.RenderTask (BlockBasedRenderer.cs:134-146) */
 static inline C3 RenderSample(const Scene& scene, const rt_render_params& P, int px, int py, int t, bool* invalid) {
     Rng rand(P.seed, (uint32_t)px, (uint32_t)py, (uint32_t)t);
@@ -338,6 +387,7 @@ static inline C3 RenderSample(const Scene& scene, const rt_render_params& P, int
     V2 sp = v2((float)px + jitter.x, (float)py + jitter.y);
     Ray ray = scene.Camera.SampleRay(sp);
     C3 color = (P.integrator == RT_INTEGRATOR_VOL_PATH) ? VolPathLi(scene, P, ray, rand) : PathLi(scene, P, ray, rand);
+    /* RT_INTEGRATOR_PARTICLE never gets here: the block renderer rejects it */
     *invalid = !IsValid(color);
     if (*invalid) color = c3s(0.0f);
     return color;
@@ -422,6 +472,7 @@ int or_render(void* sp, const rt_render_params* p, float* out, int threads, rt_s
     const Scene* s = (const Scene*)sp;
     int x0, y0, w, h;
     if (!s || !p || !out || p->spp <= 0 || !Crop(s, p, &x0, &y0, &w, &h)) return RT_ERR_INVALID_ARG;
+    if (p->integrator == RT_INTEGRATOR_PARTICLE) return RT_ERR_INVALID_ARG;
     int nthreads = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
     if (nthreads <= 0) nthreads = 1;
     std::vector<Counters> counters(nthreads);
@@ -473,6 +524,108 @@ int or_render_samples(void* sp, const rt_render_params* p, float* out, int threa
             C3 c = RenderSample(*s, *p, x0 + lx, y0 + ly, p->sample_begin + t, &inv);
             float* o = out + (((size_t)lx * h + ly) * p->spp + t) * 3;
             o[0] = c.r; o[1] = c.g; o[2] = c.b;
+        }
+    });
+    return RT_OK;
+}
+
+static inline Rng ParticleRng(uint64_t seed, int64_t i) {
+    return Rng(seed, (uint32_t)(uint64_t)i, (uint32_t)((uint64_t)i >> 32), RT_PARTICLE_STREAM);
+}
+static bool ParticleArgs(const Scene* s, const rt_render_params* p, int64_t first, int64_t count) {
+    return s && p && p->integrator == RT_INTEGRATOR_PARTICLE && first >= 0 && count > 0 &&
+           p->x0 == 0 && p->y0 == 0 && p->width == 0 && p->height == 0;
+}
+
+/* AdjointParticleRenderer (Renderers/AdjointParticleRenderer.cs:118-172): each thread
+ * takes a fixed contiguous share of the particles and splats into its own film; the
+ * films are summed in thread order, so a fixed thread count gives a fixed film. */
+int or_render_particles(void* sp, const rt_render_params* p, int64_t first, int64_t count, float* out,
+                        int threads, rt_stats* stats) {
+    const Scene* s = (const Scene*)sp;
+    if (!ParticleArgs(s, p, first, count) || !out) return RT_ERR_INVALID_ARG;
+    const int W = s->Camera.ScreenX, H = s->Camera.ScreenY;
+    const size_t npix = (size_t)W * H;
+    int nthreads = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    if (nthreads <= 0) nthreads = 1;
+    if (count < nthreads) nthreads = (int)count;
+    std::vector<std::vector<float>> films(nthreads, std::vector<float>(npix * 3, 0.0f));
+    std::vector<Counters> counters(nthreads);
+    std::vector<int> overflow(nthreads, 0);
+    auto worker = [&](int tid) {
+        tl_counters = &counters[tid];
+        std::vector<Splat> splats;
+        float* film = films[tid].data();
+        int64_t b = first + count * tid / nthreads, e = first + count * (tid + 1) / nthreads;
+        for (int64_t i = b; i < e; i++) {
+            Rng rand = ParticleRng(p->seed, i);
+            splats.clear();
+            tl_stack_overflow = false;
+            EmitParticle(*s, *p, rand, &splats);
+            if (tl_stack_overflow) overflow[tid] = 1;
+            for (const Splat& q : splats) {
+                if (q.x < 0 || q.x >= W || q.y < 0 || q.y >= H) continue;
+                float* o = film + ((size_t)q.x * H + q.y) * 3;
+                o[0] = o[0] + q.color.r; o[1] = o[1] + q.color.g; o[2] = o[2] + q.color.b;
+            }
+        }
+        tl_counters = nullptr;
+    };
+    std::vector<std::thread> ts;
+    for (int t = 1; t < nthreads; t++) ts.emplace_back(worker, t);
+    worker(0);
+    for (auto& t : ts) t.join();
+    /* film sums, then RefRGB *= v and += CameraTraceLight(SampleRay(x, y)) */
+    const float v = (float)W * (float)H / (float)count;
+    int fthreads = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    std::vector<Counters> fcount(fthreads > 0 ? fthreads : 1);
+    ParallelFor((int64_t)npix, threads, [&](int64_t q, int tid) {
+        tl_counters = &fcount[tid];
+        int x = (int)(q / H), y = (int)(q % H);
+        C3 sum = c3s(0.0f);
+        for (int t = 0; t < nthreads; t++) {
+            const float* f = films[t].data() + (size_t)q * 3;
+            sum = sum + c3(f[0], f[1], f[2]);
+        }
+        C3 c = sum * v;
+        c = c + CameraTraceLight(*s, s->Camera.SampleRay(v2((float)x, (float)y)));
+        out[q * 3] = c.r; out[q * 3 + 1] = c.g; out[q * 3 + 2] = c.b;
+        tl_counters = nullptr;
+    });
+    for (const Counters& f : fcount) counters.push_back(f);
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->samples = (uint64_t)count;
+        for (size_t i = 0; i < counters.size(); i++) {
+            stats->rays_closest += counters[i].rays_closest; stats->rays_shadow += counters[i].rays_shadow;
+            stats->node_visits += counters[i].node_visits; stats->prim_tests += counters[i].prim_tests;
+            stats->instance_visits += counters[i].instance_visits;
+        }
+    }
+    for (int t = 0; t < nthreads; t++) if (overflow[t]) return RT_ERR_STACK;
+    return RT_OK;
+}
+
+/* the camera connections of each particle, in emission order (parity hook) */
+int or_particle_splats(void* sp, const rt_render_params* p, int64_t first, int64_t count, int max_per,
+                       int32_t* n, int32_t* pix, float* rgb, int threads) {
+    const Scene* s = (const Scene*)sp;
+    if (!ParticleArgs(s, p, first, count) || max_per < 0 || !n || (max_per > 0 && (!pix || !rgb)))
+        return RT_ERR_INVALID_ARG;
+    const int H = s->Camera.ScreenY;
+    ParallelFor(count, threads, [&](int64_t i, int) {
+        std::vector<Splat> splats;
+        Rng rand = ParticleRng(p->seed, first + i);
+        EmitParticle(*s, *p, rand, &splats);
+        n[i] = (int32_t)splats.size();
+        for (int k = 0; k < max_per; k++) {
+            int64_t o = i * max_per + k;
+            if (k < (int)splats.size()) {
+                pix[o] = splats[k].x * H + splats[k].y;
+                rgb[o * 3] = splats[k].color.r; rgb[o * 3 + 1] = splats[k].color.g; rgb[o * 3 + 2] = splats[k].color.b;
+            } else {
+                pix[o] = -1; rgb[o * 3] = rgb[o * 3 + 1] = rgb[o * 3 + 2] = 0.0f;
+            }
         }
     });
     return RT_OK;

@@ -652,7 +652,9 @@ static inline SampleBxdfResult LambSample(C3 R, V3 wo, Rng& rand) {
 }
 
 /* ---- materials ------------------------------------------------------------------------ */
-static C3 GlassFr(const Material& m, V3 wo, V3 wi, V2 uv, const Dist& dist) { /* RoughGlass.FrImpl */
+/* `importance`: TransportMode.Importance (Material.cs:6-10) drops the 1/eta^2
+ * radiance scaling of refraction (RoughGlass.cs:63,161, FresnelSpecularBsdf.cs:58) */
+static C3 GlassFr(const Material& m, V3 wo, V3 wi, V2 uv, const Dist& dist, bool importance) { /* RoughGlass.FrImpl */
     C3 r = m.R->Sample(uv), t = m.T->Sample(uv);
     bool isReflect = SameHemisphere(wo, wi);
     bool entering = CosTheta(wo) > 0;
@@ -670,7 +672,7 @@ static C3 GlassFr(const Material& m, V3 wo, V3 wi, V2 uv, const Dist& dist) { /*
         bsdf = r * (d * g * f / (4.0f * CosTheta(wi) * CosTheta(wo)));
     } else {
         if (Dot(wo, wh) * Dot(wi, wh) > 0) return c3s(0);
-        float factor = 1 / eta;
+        float factor = importance ? 1.0f : 1 / eta;
         bsdf = (1 - f) * t * Abs(d * g * eta * eta * AbsDot(wi, wh) * AbsDot(wo, wh) * factor * factor /
                                   (CosTheta(wo) * CosTheta(wi) * sqrtDenom * sqrtDenom));
     }
@@ -702,7 +704,7 @@ static float GlassPdf(const Material& m, V3 wo, V3 wi, const Dist& dist) { /* Ro
     }
     return (isinf_(pdf) || isnan_(pdf)) ? 0.0f : pdf;
 }
-static SampleBxdfResult GlassSample(const Material& m, V3 wo, V2 uv, Rng& rand, const Dist& dist) { /* RoughGlass.SampleImpl */
+static SampleBxdfResult GlassSample(const Material& m, V3 wo, V2 uv, Rng& rand, const Dist& dist, bool importance) { /* RoughGlass.SampleImpl */
     SampleBxdfResult res;
     C3 r = m.R->Sample(uv), t = m.T->Sample(uv);
     V3 wh = dist.SampleWh(wo, rand);
@@ -731,7 +733,7 @@ static SampleBxdfResult GlassSample(const Material& m, V3 wo, V2 uv, Rng& rand, 
         eta = 1;
     }
     float sqrtDenom = Dot(wo, wh) + eta * Dot(wi, wh);
-    float factor = 1 / eta;
+    float factor = importance ? 1.0f : 1 / eta;
     float d = dist.D(wh);
     float g = dist.G(wo, wi);
     C3 btdf = (1 - f) * t * Abs(d * g * eta * eta * AbsDot(wi, wh) * AbsDot(wo, wh) * factor * factor /
@@ -761,7 +763,7 @@ static float PlasticPdf(const Material& m, V3 wo, V3 wi, const Dist& dist, C3 r)
     return (1 - p) * diffuse + p * glossy;
 }
 
-C3 Material::Fr(V3 wo, V3 wi, const Intersection& inct) const {
+C3 Material::Fr(V3 wo, V3 wi, const Intersection& inct, bool importance) const {
     switch (type) {
     case RT_MAT_DIFFUSE:
         if (OneSidedReject(*this, wo, wi)) return c3s(0.0f);
@@ -774,7 +776,7 @@ C3 Material::Fr(V3 wo, V3 wi, const Intersection& inct) const {
     }
     case RT_MAT_ROUGH_GLASS: {
         Dist d(dist, Rough->Sample(inct.UV).r, Anis->Sample(inct.UV).r);
-        return GlassFr(*this, wo, wi, inct.UV, d);
+        return GlassFr(*this, wo, wi, inct.UV, d, importance);
     }
     case RT_MAT_ROUGH_PLASTIC: {
         Dist d(dist, Rough->Sample(inct.UV).r, Anis->Sample(inct.UV).r);
@@ -807,7 +809,7 @@ float Material::Pdf(V3 wo, V3 wi, const Intersection& inct) const {
         return 0.0f;
     }
 }
-SampleBxdfResult Material::Sample(V3 wo, const Intersection& inct, Rng& rand) const {
+SampleBxdfResult Material::Sample(V3 wo, const Intersection& inct, Rng& rand, bool importance) const {
     SampleBxdfResult res;
     switch (type) {
     case RT_MAT_DIFFUSE:
@@ -821,7 +823,7 @@ SampleBxdfResult Material::Sample(V3 wo, const Intersection& inct, Rng& rand) co
     }
     case RT_MAT_ROUGH_GLASS: {
         Dist d(dist, Rough->Sample(inct.UV).r, Anis->Sample(inct.UV).r);
-        return GlassSample(*this, wo, inct.UV, rand, d);
+        return GlassSample(*this, wo, inct.UV, rand, d, importance);
     }
     case RT_MAT_ROUGH_PLASTIC: {
         Dist d(dist, Rough->Sample(inct.UV).r, Anis->Sample(inct.UV).r);
@@ -863,7 +865,7 @@ SampleBxdfResult Material::Sample(V3 wo, const Intersection& inct, Rng& rand) co
         V3 wi;
         if (!Refract(wo, n, etaI / etaT, &wi) || CosTheta(wi) == 0.0f) return res;
         C3 ft = T_ * (1.0f - f);
-        ft = ft * ((etaI * etaI) / (etaT * etaT));
+        if (!importance) ft = ft * ((etaI * etaI) / (etaT * etaT));
         ft = ft / AbsCosTheta(wi);
         res.Wi = wi; res.Fr = ft; res.Pdf = 1 - f; res.Type = Transmission | Specular;
         return res;
@@ -1012,6 +1014,36 @@ SampleLightResult InfiniteAreaLight::SampleLi(LightEvalParam inct, Rng& rand) co
     return r;
 }
 
+/* DiffuseAreaLight.SampleEmit (DiffuseAreaLight.cs:70-77) */
+LightEmitResult AreaLight::SampleEmit(Rng& rand) const {
+    float pdfPos;
+    ShapeSurfacePoint samplePoint = S->Sample(rand, &pdfPos);
+    V3 localW = Normalize(SquareToCosineHemisphere(rand.NextVec2()));
+    float pdfDir = SquareToCosineHemispherePdf(localW);
+    V3 w = samplePoint.Shading.ToWorld(localW);
+    LightEmitResult r;
+    r.Pos = samplePoint.P; r.Dir = Normalize(w); r.Normal = samplePoint.Shading.Z; r.UV = samplePoint.UV;
+    r.Radiance = LightEmit; r.PdfPos = pdfPos; r.PdfDir = pdfDir;
+    return r;
+}
+/* InfiniteAreaLight.SampleEmit (InfiniteAreaLight.cs:122-133): a direction from the
+ * map's distribution, a position on the disk of the world bounding sphere facing it */
+LightEmitResult InfiniteAreaLight::SampleEmit(Rng& rand) const {
+    V2 uv; V3 worldDir; float pdfDir;
+    SampleLightDir(rand, &uv, &worldDir, &pdfDir);
+    C3 radiance = Map->Sample(uv);
+    V3 normal = -worldDir;
+    Coordinate coord(normal);
+    V2 cd = SquareToConcentricDisk(rand.NextVec2());
+    V3 disk = WorldCenter + WorldRadius * (cd.x * coord.X + cd.y * coord.Y);
+    V3 pos = disk + worldDir * WorldRadius;
+    float pdfPos = 1 / (kPI * Sqr(WorldRadius));
+    LightEmitResult r;
+    r.Pos = pos; r.Dir = -worldDir; r.Normal = -worldDir; r.UV = uv; r.Radiance = radiance;
+    r.PdfPos = pdfPos; r.PdfDir = pdfDir;
+    return r;
+}
+
 /* ---- camera (Camera.cs:182-191) --------------------------------------------------------------- */
 Ray PerspectiveCamera::SampleRay(V2 sp) const {
     V3 ndc = v3(sp.x * InvResolve.x, sp.y * InvResolve.y, 0.0f);
@@ -1021,6 +1053,47 @@ Ray PerspectiveCamera::SampleRay(V2 sp) const {
     V3 o = Transform(v3(0, 0, 0), CameraToWorld);
     V3 d = Normalize(TransformNormal(dir, CameraToWorld));
     return Ray(o, d, Near * invZ, Far * invZ);
+}
+void PerspectiveCamera::Update() { /* Camera.cs:172-179 */
+    V3 pMin = Transform(v3(0, 0, 0), ClipToCamera);
+    V3 pMax = Transform(v3(1, 1, 0), ClipToCamera);
+    pMin = pMin / pMin.z;
+    pMax = pMax / pMax.z;
+    Min = v2(pMax.x, pMax.y);
+    Max = v2(pMin.x, pMin.y);
+    float area = Abs((Max.x - Min.x) * (Max.y - Min.y));
+    Normalization = 1 / area;
+}
+float PerspectiveCamera::Importance(V3 d) const { /* Camera.cs:193-204 */
+    float cosTheta = CosTheta(d);
+    if (cosTheta <= 0) return 0;
+    float focus = 1 / cosTheta;
+    V2 p = v2(d.x * focus, d.y * focus);
+    if (p.x < Min.x || p.x > Max.x || p.y < Min.y || p.y > Max.y) return 0.0f;
+    return Normalization * focus * focus * focus;
+}
+/* Camera.cs:221-241.  The clip-space point comes from Vector3.Transform (no w
+ * divide) and is divided by its own z, the reference's projection as written. */
+SampleCameraWiResult PerspectiveCamera::SampleWi(V3 pos) const {
+    SampleCameraWiResult r;
+    V3 localTarget = Transform(pos, WorldToCamera);
+    if (localTarget.z < Near || localTarget.z > Far) return r;
+    V3 screen = Transform(localTarget, CameraToClip);
+    screen.x = screen.x / screen.z;
+    screen.y = screen.y / screen.z;
+    screen.z = 1;
+    if (screen.x < 0 || screen.x > 1 || screen.y < 0 || screen.y > 1) return r;
+    V2 ssPos = v2(screen.x * (float)(ScreenX - 1), screen.y * (float)(ScreenY - 1));
+    float dist = Length(localTarget);
+    float inv = 1 / dist;
+    V3 localDir = localTarget * inv;
+    V3 samplePos = Transform(v3(0, 0, 0), CameraToWorld);
+    V3 dir = (samplePos - pos) / dist;
+    V3 normal = TransformNormal(v3(0, 0, 1), CameraToWorld);
+    float importance = Importance(localDir) * inv * inv;
+    r.Pos = samplePos; r.Dir = dir; r.Dist = dist; r.Normal = normal; r.Pdf = 1;
+    r.We = c3s(importance); r.ScreenPos = ssPos;
+    return r;
 }
 
 /* ---- scene services (Scene.cs) ------------------------------------------------------------------ */
@@ -1228,6 +1301,8 @@ std::unique_ptr<Scene> BuildScene(const rt_scene_desc* d, std::string* err) {
     s->Camera.ScreenX = c.width; s->Camera.ScreenY = c.height; s->Camera.Near = c.near_z; s->Camera.Far = c.far_z;
     s->Camera.ClipToCamera = ToM44(c.clip_to_camera); s->Camera.CameraToWorld = ToM44(c.camera_to_world);
     s->Camera.InvResolve = v2(1.0f / (float)c.width, 1.0f / (float)c.height);
+    s->Camera.CameraToClip = ToM44(c.camera_to_clip); s->Camera.WorldToCamera = ToM44(c.world_to_camera);
+    s->Camera.Update();
     for (InfiniteAreaLight* il : s->InfiniteLights) il->Preprocess(*s);
     return s;
 }

@@ -194,14 +194,20 @@ struct Material {
     const Texture2D *R = nullptr, *T = nullptr, *Rough = nullptr, *Anis = nullptr;
     float etaA = 1, etaB = 1, kd = 0.5f, ks = 0.5f;
     C3 Eta, K;
-    C3 Fr(V3 wo, V3 wi, const Intersection& inct) const;
+    /* importance: TransportMode.Importance instead of Radiance */
+    C3 Fr(V3 wo, V3 wi, const Intersection& inct, bool importance = false) const;
     float Pdf(V3 wo, V3 wi, const Intersection& inct) const;
-    SampleBxdfResult Sample(V3 wo, const Intersection& inct, Rng& rand) const;
+    SampleBxdfResult Sample(V3 wo, const Intersection& inct, Rng& rand, bool importance = false) const;
 };
 
 /* ---- lights: Light.cs, Lights/ -------------------------------------------- */
 struct SampleLightResult { V3 P = v3s(0); C3 Li = c3s(0); V3 Wi = v3s(0); float Pdf = 0; };
 struct LightEvalParam { V3 P; float T; };
+/* Light.cs:61-107 LightEmitResult + LightEmitPdf */
+struct LightEmitResult {
+    V3 Pos = v3s(0), Dir = v3s(0), Normal = v3s(0); V2 UV = v2(0, 0); C3 Radiance = c3s(0);
+    float PdfPos = 0, PdfDir = 0;
+};
 struct Scene;
 struct Light {
     int index = -1;
@@ -209,6 +215,7 @@ struct Light {
     bool IsDelta() const { return false; } /* Area and Infinite lights are never delta */
     virtual SampleLightResult SampleLi(LightEvalParam inct, Rng& rand) const = 0;
     virtual float PdfLi(LightEvalParam inct, V3 wi) const = 0;
+    virtual LightEmitResult SampleEmit(Rng& rand) const = 0;
     virtual C3 Le(const Ray&) const { return c3s(0); }
 };
 struct AreaLight : Light {
@@ -217,6 +224,7 @@ struct AreaLight : Light {
     C3 L(const Intersection& inct, V3 w) const { return (Dot(inct.N(), w) > 0) ? LightEmit : c3s(0); }
     SampleLightResult SampleLi(LightEvalParam inct, Rng& rand) const override;
     float PdfLi(LightEvalParam inct, V3 wi) const override;
+    LightEmitResult SampleEmit(Rng& rand) const override;
 };
 /* Distribution1D.cs / Distribution2D.cs */
 struct Distribution1D {
@@ -245,12 +253,22 @@ struct InfiniteAreaLight : Light {
     float PdfLi(LightEvalParam, V3 wi) const override { return PdfDir(wi); }
     bool SampleLightDir(Rng& rand, V2* uv, V3* dir, float* pdf) const;
     SampleLightResult SampleLi(LightEvalParam inct, Rng& rand) const override;
+    LightEmitResult SampleEmit(Rng& rand) const override;
 };
 
 /* ---- camera: Camera.cs PerspectiveCamera ---------------------------------------- */
+/* Camera.cs:21-48 SampleCameraWiResult */
+struct SampleCameraWiResult {
+    V3 Pos = v3s(0), Dir = v3s(0); float Dist = 0; V3 Normal = v3s(0); float Pdf = 0; C3 We = c3s(0);
+    V2 ScreenPos = v2(0, 0);
+};
 struct PerspectiveCamera {
     int ScreenX, ScreenY; float Near, Far; M44 ClipToCamera, CameraToWorld; V2 InvResolve;
+    M44 CameraToClip, WorldToCamera; V2 Min, Max; float Normalization;
+    void Update(); /* the _min/_max/_normalization part of Update (Camera.cs:172-179) */
     Ray SampleRay(V2 samplePosition) const;
+    float Importance(V3 d) const;
+    SampleCameraWiResult SampleWi(V3 pos) const;
 };
 
 /* ---- scene: Scene.cs ------------------------------------------------------------ */
@@ -286,6 +304,10 @@ std::unique_ptr<Scene> BuildScene(const rt_scene_desc* d, std::string* err);
 /* integrators */
 C3 PathLi(const Scene& s, const rt_render_params& p, Ray ray, Rng& rand);
 C3 VolPathLi(const Scene& s, const rt_render_params& p, Ray ray, Rng& rand);
+/* AdjointParticleIntegrator.EmitParticle: calls splat(x, y, color) per camera connection */
+struct Splat { int x, y; C3 color; };
+void EmitParticle(const Scene& s, const rt_render_params& p, Rng& rand, std::vector<Splat>* splats);
+C3 CameraTraceLight(const Scene& s, const Ray& ray);
 
 } /* namespace orc */
 

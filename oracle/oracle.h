@@ -24,6 +24,18 @@ int or_trace_any(void* s, const rt_ray* rays, int64_t n, uint8_t* occluded, int 
  * stats (nullable) receives the summed counters. */
 int or_render(void* s, const rt_render_params* p, float* out_rgb, int threads, rt_stats* stats);
 
+/* AdjointParticleRenderer: particles [first, first + count) -> the whole film
+ * (ColorBuffer layout).  Each thread splats a fixed share into its own film;
+ * the films are summed in thread order. */
+int or_render_particles(void* s, const rt_render_params* p, int64_t first, int64_t count, float* out_rgb,
+                        int threads, rt_stats* stats);
+
+/* camera connections of particles [first, first + count): n[i] of particle
+ * first + i; the first max_per at pix[i * max_per + k] (x * ScreenY + y, -1
+ * beyond n[i]) and rgb[(i * max_per + k) * 3 + c] */
+int or_particle_splats(void* s, const rt_render_params* p, int64_t first, int64_t count, int max_per,
+                       int32_t* n, int32_t* pix, float* rgb, int threads);
+
 /* per-sample radiance (no averaging): out[((x*h + y) * spp + k) * 3 + c] */
 int or_render_samples(void* s, const rt_render_params* p, float* out, int threads);
 

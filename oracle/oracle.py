@@ -39,6 +39,10 @@ def lib():
         L.or_trace_any.argtypes = [vp, vp, C.c_int64, vp, C.c_int]
         L.or_render.argtypes = [vp, C.POINTER(N.RenderParams), vp, C.c_int, C.POINTER(N.Stats)]
         L.or_render_samples.argtypes = [vp, C.POINTER(N.RenderParams), vp, C.c_int]
+        L.or_render_particles.argtypes = [vp, C.POINTER(N.RenderParams), C.c_int64, C.c_int64, vp, C.c_int,
+                                          C.POINTER(N.Stats)]
+        L.or_particle_splats.argtypes = [vp, C.POINTER(N.RenderParams), C.c_int64, C.c_int64, C.c_int, vp, vp, vp,
+                                         C.c_int]
         L.or_camera_rays.argtypes = [vp, vp, C.c_int64, vp]
         L.or_bvh.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp, vp, vp, vp, vp]
         L.or_detmath.argtypes = [C.c_int, vp, vp, vp, C.c_int64]
@@ -111,6 +115,31 @@ class OracleScene:
         if rc != 0:
             raise N.RTError(rc, "oracle render_samples")
         return out.reshape(w, h, settings.spp, 3)
+
+    def render_particles(self, settings, count: int, first: int = 0, threads: int = 0, stats: bool = False):
+        """AdjointParticleRenderer film of particles [first, first + count): (width, height, 3)."""
+        cam = self.scene.camera
+        out = np.zeros(cam.width * cam.height * 3, dtype=np.float32)
+        st = N.Stats()
+        p = settings.to_c()
+        rc = lib().or_render_particles(self.h, C.byref(p), first, count, _ptr(out), threads,
+                                       C.byref(st) if stats else None)
+        if rc != 0:
+            raise N.RTError(rc, "oracle render_particles")
+        img = out.reshape(cam.width, cam.height, 3)
+        return (img, st.as_dict()) if stats else img
+
+    def particle_splats(self, settings, count: int, max_per: int, first: int = 0, threads: int = 0):
+        """Camera connections per particle: (n[count], pix[count, max_per], rgb[count, max_per, 3])."""
+        n = np.zeros(count, dtype=np.int32)
+        pix = np.zeros((count, max_per), dtype=np.int32)
+        rgb = np.zeros((count, max_per, 3), dtype=np.float32)
+        p = settings.to_c()
+        rc = lib().or_particle_splats(self.h, C.byref(p), first, count, max_per, _ptr(n), _ptr(pix), _ptr(rgb),
+                                      threads)
+        if rc != 0:
+            raise N.RTError(rc, "oracle particle_splats")
+        return n, pix, rgb
 
     def camera_rays(self, screen_pos: np.ndarray) -> np.ndarray:
         sp = np.ascontiguousarray(screen_pos, dtype=np.float32).reshape(-1, 2)

@@ -1,7 +1,7 @@
 """Builds libradiantium_gb300.so in-tree for sm_103a.
 
 Translation units compiled in parallel and linked with nvcc:
-  rt_kernels.cu, rt_wavefront.cu, rt_adjoint.cu  device code: --fmad=false keeps every
+  rt_kernels.cu, rt_wavefront.cu, rt_adjoint.cu, rt_particles.cu  device code: --fmad=false keeps every
                  multiply and add separately rounded (the reference's
                  arithmetic), IEEE division and square root are nvcc's
                  defaults;
@@ -46,6 +46,8 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
                             "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_wavefront.cu")],
         "rt_adjoint.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_adjoint.cu")],
+        "rt_particles.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                           "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_particles.cu")],
         "rt_bvh_gpu.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                          *extra_nvcc, "-c", os.path.join(CSRC, "rt_bvh_gpu.cu")],
         "rt_noalloc.o": [nvcc, ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *extra_nvcc,

@@ -187,9 +187,12 @@ class GpuRenderer:
     Samples are rendered in progressive passes so that Stop() and the task
     counters behave like BlockBasedRenderer's blocks."""
 
-    def __init__(self, scene: SceneDesc, settings: RenderSettings, device: int = 0, passes: int = 0):
+    def __init__(self, scene: SceneDesc, settings: RenderSettings, device: int = 0, passes: int = 0,
+                 particle_count: int = 0):
         self.scene, self.settings, self.device = scene, settings, device
-        self.passes = passes or min(settings.spp, 16)
+        self.particle_count = particle_count
+        work = particle_count if settings.integrator == N.INTEGRATOR_PARTICLE else settings.spp
+        self.passes = passes or min(work, 16)
         self._target = np.zeros((scene.camera.width, scene.camera.height, 3), dtype=np.float32)
         self._thread = None
         self._done = 0
@@ -252,6 +255,10 @@ class GpuRenderer:
                 dev.upload(self.scene)
                 st = self.settings
                 acc = np.zeros_like(self._target, dtype=np.float64)
+                if st.integrator == N.INTEGRATOR_PARTICLE:
+                    self._run_particles(dev, acc)
+                    self._dev = None
+                    return
                 done_spp = 0
                 per = [st.spp // self.passes + (1 if i < st.spp % self.passes else 0) for i in range(self.passes)]
                 for k in per:
@@ -267,6 +274,20 @@ class GpuRenderer:
             self._error = e
         finally:
             self._t1 = time.perf_counter()
+
+    def _run_particles(self, dev, acc):
+        """AdjointParticleRenderer: particle ranges per pass; a film of n particles
+        weighs n / N in the running mean (each film is already scaled by 1/n)."""
+        n_all, done = self.particle_count, 0
+        per = [n_all // self.passes + (1 if i < n_all % self.passes else 0) for i in range(self.passes)]
+        for k in per:
+            if self._stop.is_set() or k == 0:
+                break
+            img = dev.render_particles(self.settings, k, first=done)
+            acc += img.astype(np.float64) * k
+            done += k
+            self._done += 1
+            self._target[...] = (acc / done).astype(np.float32)
 
 
 class RendererBuilder:
@@ -295,7 +316,11 @@ class RendererBuilder:
             return RenderSettings(N.INTEGRATOR_VOL_PATH, N.METHOD_MIS, strat, p.int("max_depth", -1),
                                   p.int("min_depth", 3), p.float("rr_threshold", 0.99))
 
-        self.integrators.update({"path": path, "vol_path": vol_path})
+        def adjoint_particle(b, p):
+            return RenderSettings(N.INTEGRATOR_PARTICLE, N.METHOD_MIS, N.STRATEGY_UNIFORM, p.int("max_depth", -1),
+                                  p.int("min_depth", 3), p.float("rr_threshold", 0.99))
+
+        self.integrators.update({"path": path, "vol_path": vol_path, "adjoint_particle": adjoint_particle})
         self.accels["bvh"] = lambda b, p: max(1, p.int("max_prim", 1))
 
         def dist(p, default):
@@ -346,6 +371,7 @@ class RendererBuilder:
         self.shapes["sphere"] = lambda b, m, p: (p.vec3("center", (0.0, 0.0, 0.0)), p.float("radius", 0.5), m)
         for name in ("block_based", "gpu_wavefront"):
             self.renderers[name] = lambda b, p: (p.int("spp", 256), p.int("block_size", 32), p.int("threads", -1))
+        self.renderers["adjoint_particle"] = lambda b, p: (p.int("particle_count", 16384), p.int("threads", -1))
         return self
 
     # -- texture parameter (RendererBuilderExtension.ReadTex2D) ------------------------------------
@@ -542,10 +568,11 @@ class RendererBuilder:
         if ic is None or ic.str("type", None) not in self.integrators:
             raise NotImplementedError(f"integrator {None if ic is None else ic.str('type', None)}")
         settings = self.integrators[ic.str("type", None)](self, ic)
-        spp = 256
-        if self.renderer_cfg is not None:
-            spp = self.renderers["block_based"](self, self.renderer_cfg)[0]
-        settings = settings.replace(spp=spp)
+        rc = self.renderer_cfg if self.renderer_cfg is not None else ConfigParams()
+        if settings.integrator == N.INTEGRATOR_PARTICLE:
+            # the renderer named by the integrator (AdjointParticleIntegrator.cs:15, RendererBuilder.cs:523)
+            return GpuRenderer(s, settings, device, particle_count=self.renderers["adjoint_particle"](self, rc)[0])
+        settings = settings.replace(spp=self.renderers["block_based"](self, rc)[0])
         return GpuRenderer(s, settings, device)
 
 

@@ -642,6 +642,23 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     cam.inv_res_x = 1.0f / (float)cam.width; cam.inv_res_y = 1.0f / (float)cam.height;
     std::memcpy(cam.clip_to_camera, d->camera.clip_to_camera, sizeof(cam.clip_to_camera));
     std::memcpy(cam.camera_to_world, d->camera.camera_to_world, sizeof(cam.camera_to_world));
+    std::memcpy(cam.camera_to_clip, d->camera.camera_to_clip, sizeof(cam.camera_to_clip));
+    std::memcpy(cam.world_to_camera, d->camera.world_to_camera, sizeof(cam.world_to_camera));
+    {   /* PerspectiveCamera.Update (Camera.cs:172-179): the image plane at z = 1 */
+        const float* m = cam.clip_to_camera;
+        auto xf = [m](float x, float y, float z, float* o) {
+            for (int k = 0; k < 3; k++) o[k] = x * m[k] + y * m[4 + k] + z * m[8 + k] + m[12 + k];
+        };
+        float pmin[3], pmax[3];
+        xf(0, 0, 0, pmin);
+        xf(1, 1, 0, pmax);
+        const float zmin = pmin[2], zmax = pmax[2];
+        for (int k = 0; k < 3; k++) { pmin[k] = pmin[k] / zmin; pmax[k] = pmax[k] / zmax; }
+        cam.min_x = pmax[0]; cam.min_y = pmax[1];
+        cam.max_x = pmin[0]; cam.max_y = pmin[1];
+        const float area = std::fabs((cam.max_x - cam.min_x) * (cam.max_y - cam.min_y));
+        cam.normalization = 1 / area;
+    }
     c->d_view = upload(c, std::vector<RtSceneView>{v});
     CK(cudaStreamSynchronize(c->stream));
     c->has_scene = true;
@@ -744,6 +761,95 @@ void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t
     c->last.shade_kernel_ms = 0;
     c->last.render_launches = (uint64_t)nchunks;
     c->last.kernel_launches = launches;
+}
+
+/* RtParams of a light-tracing call (whole film) */
+RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64_t count) {
+    if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+    if (!p) throw RtFail(RT_ERR_INVALID_ARG, "render_particles: null params");
+    if (p->integrator != RT_INTEGRATOR_PARTICLE)
+        throw RtFail(RT_ERR_INVALID_ARG, "render_particles: the integrator must be RT_INTEGRATOR_PARTICLE");
+    if (p->x0 != 0 || p->y0 != 0 || p->width != 0 || p->height != 0)
+        throw RtFail(RT_ERR_INVALID_ARG, "render_particles: particles splat into the whole film (crop fields must be 0)");
+    if (first < 0 || count <= 0 || first > INT64_MAX - count)
+        throw RtFail(RT_ERR_INVALID_ARG, "render_particles: bad particle range");
+    RtParams P{};
+    P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
+    P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;
+    P.seed = p->seed; P.w = c->width; P.h = c->height;
+    return P;
+}
+
+/* AdjointParticleRenderer (Renderers/AdjointParticleRenderer.cs:118-172): the
+ * particles in launches of up to sample_budget, then the finishing pass */
+void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t count, float* dst, bool dst_host,
+                      cudaStream_t user) {
+    RtParams P = particle_params(c, p, first, count);
+    if (!dst) throw RtFail(RT_ERR_INVALID_ARG, "render_particles: null output");
+    cudaStream_t s = user ? user : c->stream;
+    const int64_t npix = (int64_t)P.w * P.h;
+    ensure(&c->film, &c->film_bytes, (size_t)npix * 12);
+    CK(cudaMemsetAsync(c->film, 0, (size_t)npix * 12, s));
+    CK(cudaMemsetAsync(c->status, 0, 4, s));
+    CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
+    c->cancel.store(0);
+    const int64_t chunk = std::max<int64_t>(1, c->sample_budget);
+    const int64_t nchunks = (count + chunk - 1) / chunk;
+    ensure_events(c, 2 * (size_t)nchunks);
+    for (int64_t b = 0, ci = 0; b < count; b += chunk, ci++) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        CK(cudaEventRecord(c->events[2 * ci], s));
+        CK(rt_launch_particles(c->d_view, P, first + b, std::min(chunk, count - b), c->film, c->status, c->stats,
+                               c->counting, s));
+        CK(cudaEventRecord(c->events[2 * ci + 1], s));
+    }
+    float* out = dst;
+    if (dst_host) {
+        ensure(&c->out, &c->out_bytes, (size_t)npix * 12);
+        out = c->out;
+    }
+    /* float v = (float)ScreenX * ScreenY / pathCount (AdjointParticleRenderer.cs:156-157) */
+    const float v = (float)P.w * (float)P.h / (float)count;
+    CK(rt_launch_particle_finish(c->d_view, npix, c->film, v, out, c->status, c->stats, c->counting, s));
+    if (dst_host) CK(cudaMemcpyAsync(dst, out, (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    check_status(c);
+    double ms = 0;
+    for (int64_t ci = 0; ci < nchunks; ci++) {
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, c->events[2 * ci], c->events[2 * ci + 1]));
+        ms += t;
+    }
+    std::memset(&c->last, 0, sizeof(c->last));
+    read_stats(c);
+    c->last.samples = (uint64_t)count;
+    c->last.render_kernel_ms = ms;
+    c->last.render_launches = (uint64_t)nchunks;
+    c->last.kernel_launches = (uint64_t)nchunks + 1;
+}
+
+/* parity hook: each particle's camera connections into host arrays */
+void particle_splats(Ctx* c, const rt_render_params* p, int64_t first, int64_t count, int max_per, int32_t* n,
+                     int32_t* pix, float* rgb) {
+    RtParams P = particle_params(c, p, first, count);
+    if (max_per < 0 || !n || (max_per > 0 && (!pix || !rgb)) || count > (int64_t)1 << 26)
+        throw RtFail(RT_ERR_INVALID_ARG, "particle_splats: bad output");
+    const size_t nb = (size_t)count * 4, pb = (size_t)count * max_per * 4, rb = pb * 3;
+    char* buf = nullptr;
+    CK(cudaMalloc((void**)&buf, nb + pb + rb + 16));
+    struct Free { char* b; ~Free() { cudaFree(b); } } guard{buf};
+    int32_t* dn = (int32_t*)buf;
+    int32_t* dp = (int32_t*)(buf + nb);
+    float* dr = (float*)(buf + nb + pb);
+    CK(cudaMemsetAsync(c->status, 0, 4, c->stream));
+    CK(rt_launch_particle_records(c->d_view, P, first, count, dn, dp, dr, max_per, c->status, c->stream));
+    CK(cudaMemcpyAsync(n, dn, nb, cudaMemcpyDeviceToHost, c->stream));
+    if (max_per > 0) {
+        CK(cudaMemcpyAsync(pix, dp, pb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(rgb, dr, rb, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    check_status(c);
 }
 
 /* rt_render_device_noalloc: the megakernel render with every buffer carved
@@ -1310,6 +1416,18 @@ int rt_render(void* ctx, const rt_render_params* params, float* out_rgb) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render(c, params, out_rgb, true, nullptr); });
 }
+int rt_render_particles(void* ctx, const rt_render_params* params, int64_t first_particle, int64_t particle_count,
+                        float* out_rgb) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { render_particles(c, params, first_particle, particle_count, out_rgb, true, nullptr); });
+}
+int rt_render_particles_device(void* ctx, const rt_render_params* params, int64_t first_particle,
+                               int64_t particle_count, float* d_out_rgb, void* stream) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() {
+        render_particles(c, params, first_particle, particle_count, d_out_rgb, false, (cudaStream_t)stream);
+    });
+}
 int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb, void* stream) {
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() { render(c, params, d_out_rgb, false, (cudaStream_t)stream); });
@@ -1375,6 +1493,13 @@ int rt_cancel(void* ctx) {
 /* test hook (not in the public header): shrinks the samples per round and
  * the path slots in flight so small renders exercise several rounds and
  * heavy slot reuse; 0 keeps a value */
+/* test hook (not part of radiantium.h): each particle's camera connections,
+ * laid out like the oracle's or_particle_splats */
+int rt_debug_particle_splats(void* ctx, const rt_render_params* params, int64_t first, int64_t count, int max_per,
+                             int32_t* n, int32_t* pix, float* rgb) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() { particle_splats(c, params, first, count, max_per, n, pix, rgb); });
+}
 int rt_debug_set_limits(void* ctx, int64_t sample_budget, int wf_capacity) {
     Ctx* c = (Ctx*)ctx;
     if (!c || sample_budget < 0 || wf_capacity < 0) return RT_ERR_INVALID_ARG;

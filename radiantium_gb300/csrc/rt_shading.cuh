@@ -209,7 +209,9 @@ DF BSample LambSample(C3 R, V3 wo, Rng& rand) {
     return r;
 }
 
-/* RoughGlass (Materials/RoughGlass.cs) */
+/* RoughGlass (Materials/RoughGlass.cs).  kImp: TransportMode.Importance, which
+ * drops the 1/eta^2 scaling of refraction (RoughGlass.cs:63,161). */
+template <bool kImp = false>
 DF C3 GlassFr(const RtSceneView* S, const RtMaterial& m, V3 wo, V3 wi, V2 uv, const Dist& dist) {
     C3 r = TexSample(S, m.tex_r, uv), t = TexSample(S, m.tex_t, uv);
     bool isReflect = SameHemisphere(wo, wi);
@@ -228,7 +230,7 @@ DF C3 GlassFr(const RtSceneView* S, const RtMaterial& m, V3 wo, V3 wi, V2 uv, co
         bsdf = r * (d * g * f / (4.0f * CosTheta(wi) * CosTheta(wo)));
     } else {
         if (Dot(wo, wh) * Dot(wi, wh) > 0) return c3s(0);
-        float factor = 1 / eta;
+        float factor = kImp ? 1.0f : 1 / eta;
         bsdf = (1 - f) * t * Abs(d * g * eta * eta * AbsDot(wi, wh) * AbsDot(wo, wh) * factor * factor /
                                   (CosTheta(wo) * CosTheta(wi) * sqrtDenom * sqrtDenom));
     }
@@ -260,6 +262,7 @@ DF float GlassPdf(const RtMaterial& m, V3 wo, V3 wi, const Dist& dist) {
     }
     return (isinff_(pdf) || isnanf_(pdf)) ? 0.0f : pdf;
 }
+template <bool kImp = false>
 DF BSample GlassSample(const RtSceneView* S, const RtMaterial& m, V3 wo, V2 uv, Rng& rand, const Dist& dist) {
     BSample res = empty_sample();
     C3 r = TexSample(S, m.tex_r, uv), t = TexSample(S, m.tex_t, uv);
@@ -289,7 +292,7 @@ DF BSample GlassSample(const RtSceneView* S, const RtMaterial& m, V3 wo, V2 uv, 
         eta = 1;
     }
     float sqrtDenom = Dot(wo, wh) + eta * Dot(wi, wh);
-    float factor = 1 / eta;
+    float factor = kImp ? 1.0f : 1 / eta;
     float d = DistD(dist, wh);
     float g = DistG(dist, wo, wi);
     C3 btdf = (1 - f) * t * Abs(d * g * eta * eta * AbsDot(wi, wh) * AbsDot(wo, wh) * factor * factor /
@@ -320,7 +323,8 @@ DF Dist MatDist(const RtSceneView* S, const RtMaterial& m, V2 uv) {
     return mkdist(m.dist, TexSample(S, m.tex_rough, uv).r, TexSample(S, m.tex_anis, uv).r);
 }
 
-/* Material.Fr (Material.cs:28) */
+/* Material.Fr (Material.cs:28); kImp: TransportMode.Importance */
+template <bool kImp = false>
 NF C3 MatFr(const RtSceneView* S, int mi, V3 wo, V3 wi, V2 uv) {
     const RtMaterial m = S->materials[mi];
     switch (m.type) {
@@ -333,7 +337,7 @@ NF C3 MatFr(const RtSceneView* S, int mi, V3 wo, V3 wi, V2 uv) {
         MicroRefl mr{c3s(1.0f), 0, c3(m.eta[0], m.eta[1], m.eta[2]), c3(m.k[0], m.k[1], m.k[2]), 0, 0, d};
         return MRFr(mr, wo, wi);
     }
-    case RT_MAT_ROUGH_GLASS: return GlassFr(S, m, wo, wi, uv, MatDist(S, m, uv));
+    case RT_MAT_ROUGH_GLASS: return GlassFr<kImp>(S, m, wo, wi, uv, MatDist(S, m, uv));
     case RT_MAT_ROUGH_PLASTIC: return PlasticFr(m, wo, wi, MatDist(S, m, uv), TexSample(S, m.tex_r, uv));
     default: return c3s(0.0f);
     }
@@ -356,7 +360,8 @@ NF float MatPdf(const RtSceneView* S, int mi, V3 wo, V3 wi, V2 uv) {
     default: return 0.0f;
     }
 }
-/* Material.Sample (Material.cs:38) */
+/* Material.Sample (Material.cs:38); kImp: TransportMode.Importance */
+template <bool kImp = false>
 NF BSample MatSample(const RtSceneView* S, int mi, V3 wo, V2 uv, Rng& rand) {
     const RtMaterial m = S->materials[mi];
     BSample res = empty_sample();
@@ -370,7 +375,7 @@ NF BSample MatSample(const RtSceneView* S, int mi, V3 wo, V2 uv, Rng& rand) {
         MicroRefl mr{c3s(1.0f), 0, c3(m.eta[0], m.eta[1], m.eta[2]), c3(m.k[0], m.k[1], m.k[2]), 0, 0, d};
         return MRSample(mr, wo, rand);
     }
-    case RT_MAT_ROUGH_GLASS: return GlassSample(S, m, wo, uv, rand, MatDist(S, m, uv));
+    case RT_MAT_ROUGH_GLASS: return GlassSample<kImp>(S, m, wo, uv, rand, MatDist(S, m, uv));
     case RT_MAT_ROUGH_PLASTIC: {
         Dist d = MatDist(S, m, uv);
         if (CosTheta(wo) <= 0 && !m.two_sided) return res;
@@ -411,7 +416,7 @@ NF BSample MatSample(const RtSceneView* S, int mi, V3 wo, V2 uv, Rng& rand) {
         V3 wi;
         if (!Refract(wo, n, etaI / etaT, &wi) || CosTheta(wi) == 0.0f) return res;
         C3 ft = T * (1.0f - f);
-        ft = ft * ((etaI * etaI) / (etaT * etaT));
+        if (!kImp) ft = ft * ((etaI * etaI) / (etaT * etaT)); /* FresnelSpecularBsdf.cs:58-61 */
         ft = ft / AbsCosTheta(wi);
         res.Wi = wi; res.Fr = ft; res.Pdf = 1 - f; res.Type = BX_TRANSMISSION | BX_SPECULAR;
         return res;
@@ -708,6 +713,107 @@ DF Ray CameraRay(const RtCamera& cam, V2 sp) {
     V3 o = Xf16(v3(0, 0, 0), cam.camera_to_world);
     V3 d = Normalize(XfN16(dir, cam.camera_to_world));
     return mkray(o, d, cam.near_z * invZ, cam.far_z * invZ);
+}
+
+/* ---- light tracing: Light.SampleEmit and PerspectiveCamera.SampleWi -------------------- */
+/* Probability.SquareToConcentricDisk (Probability.cs:157-174) */
+DF V2 SquareToConcentricDisk(V2 u) {
+    V2 uOffset = v2(2.0f * u.x - 1.0f, 2.0f * u.y - 1.0f);
+    if (uOffset.x == 0 && uOffset.y == 0) return v2(0, 0);
+    float theta, r;
+    if (Abs(uOffset.x) > Abs(uOffset.y)) {
+        r = uOffset.x;
+        theta = (kPI / 4) * (uOffset.y / uOffset.x);
+    } else {
+        r = uOffset.y;
+        theta = (kPI / 2) - (kPI / 4) * (uOffset.x / uOffset.y);
+    }
+    float sinTheta = rt_sinf(theta), cosTheta = rt_cosf(theta);
+    return v2(r * cosTheta, r * sinTheta);
+}
+/* LightEmitResult (Light.cs:61-107) without the unused uv */
+struct Emit { V3 pos, dir, n; C3 le; float pdf_pos, pdf_dir; };
+/* Light.SampleEmit: DiffuseAreaLight.cs:70-77, InfiniteAreaLight.cs:122-133 */
+NF Emit LightSampleEmit(const RtSceneView* S, int li, Rng& rand) {
+    const RtLight& L = S->lights[li];
+    Emit e;
+    if (L.kind == RT_LIGHT_INFINITE) {
+        /* SampleLightDir (InfiniteAreaLight.cs:92-109): a zero direction and pdf 0
+         * when the sample fails, which SampleEmit passes on unchecked */
+        const RtDist2D d = S->dists[L.dist];
+        float pdf; int ov, ou;
+        Sample2D(S, d, NextVec2(rand), &pdf, &ov, &ou);
+        V2 uv = v2(0, 0);
+        V3 worldDir = v3s(0);
+        float pdfDir = 0;
+        if (pdf > 0) {
+            float y = (float)ov / (float)d.nv;
+            float x = (float)ou / (float)d.nu;
+            uv = v2(x, y);
+            float theta = y * kPI;
+            float phi = x * 2 * kPI;
+            float sinTheta = rt_sinf(theta);
+            if (sinTheta != 0) {
+                pdf /= (2 * kPI * kPI * sinTheta);
+                float cosTheta = rt_cosf(theta);
+                float sinPhi = rt_sinf(phi), cosPhi = rt_cosf(phi);
+                V3 sph = v3(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
+                V3 dir = v3(sph.y, sph.z, -sph.x);
+                worldDir = Normalize(XfN12(dir, L.m2w));
+                pdfDir = pdf;
+            }
+        }
+        C3 radiance = TexSample(S, L.ref, uv);
+        V3 normal = -worldDir;
+        Frame coord = mkframe(normal);
+        V2 cd = SquareToConcentricDisk(NextVec2(rand));
+        V3 center = v3(L.world_center[0], L.world_center[1], L.world_center[2]);
+        V3 disk = center + L.world_radius * (cd.x * coord.X + cd.y * coord.Y);
+        e.pos = disk + worldDir * L.world_radius;
+        e.dir = -worldDir; e.n = -worldDir; e.le = radiance;
+        e.pdf_pos = 1 / (kPI * (L.world_radius * L.world_radius));
+        e.pdf_dir = pdfDir;
+        return e;
+    }
+    V3 sp, sn; float pdfPos;
+    ShapeSample(S, L, rand, &sp, &sn, &pdfPos);
+    V3 localW = Normalize(SquareToCosineHemisphere(NextVec2(rand)));
+    float pdfDir = CosTheta(localW) / kPI; /* SquareToCosineHemispherePdf */
+    Frame F = mkframe(sn);
+    e.pos = sp; e.dir = Normalize(ToWorld(F, localW)); e.n = sn;
+    e.le = c3(L.le[0], L.le[1], L.le[2]);
+    e.pdf_pos = pdfPos; e.pdf_dir = pdfDir;
+    return e;
+}
+/* PerspectiveCamera.Importance (Camera.cs:193-204); d normalized, camera space */
+DF float CameraImportance(const RtCamera& cam, V3 d) {
+    float cosTheta = CosTheta(d);
+    if (cosTheta <= 0) return 0;
+    float focus = 1 / cosTheta;
+    float px = d.x * focus, py = d.y * focus;
+    if (px < cam.min_x || px > cam.max_x || py < cam.min_y || py > cam.max_y) return 0.0f;
+    return cam.normalization * focus * focus * focus;
+}
+/* SampleCameraWiResult (Camera.cs:21-48) fields the light tracer reads; pdf is 1 */
+struct CamWi { V3 pos, dir; float we, sx, sy; };
+/* PerspectiveCamera.SampleWi (Camera.cs:221-241); false where it returns the
+ * empty result (pdf 0).  The clip-space point comes from Vector3.Transform (no
+ * w divide) and is divided by its own z, the reference's projection as written. */
+DF bool CameraSampleWi(const RtCamera& cam, V3 pos, CamWi* r) {
+    V3 lt = Xf16(pos, cam.world_to_camera);
+    if (lt.z < cam.near_z || lt.z > cam.far_z) return false;
+    V3 screen = Xf16(lt, cam.camera_to_clip);
+    float sx = screen.x / screen.z, sy = screen.y / screen.z;
+    if (sx < 0 || sx > 1 || sy < 0 || sy > 1) return false;
+    r->sx = sx * (float)(cam.width - 1);
+    r->sy = sy * (float)(cam.height - 1);
+    float dist = Length(lt);
+    float inv = 1 / dist;
+    V3 localDir = lt * inv;
+    r->pos = Xf16(v3(0, 0, 0), cam.camera_to_world);
+    r->dir = (r->pos - pos) / dist;
+    r->we = CameraImportance(cam, localDir) * inv * inv;
+    return true;
 }
 
 }  /* namespace rtd */

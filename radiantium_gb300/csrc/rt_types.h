@@ -130,6 +130,10 @@ struct RtCamera {
     float inv_res_x, inv_res_y;
     float clip_to_camera[16];
     float camera_to_world[16];
+    float camera_to_clip[16];       /* light tracing (PerspectiveCamera.SampleWi) */
+    float world_to_camera[16];
+    float min_x, min_y, max_x, max_y; /* _min, _max of the z = 1 image plane (Camera.cs:172-177) */
+    float normalization;            /* _normalization = 1 / its area (Camera.cs:178-179) */
 };
 
 /* pointers handed to the kernels by value */

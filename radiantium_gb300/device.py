@@ -101,6 +101,33 @@ class Device:
         p = settings.to_c()
         self._check(self.lib.rt_render_device(self.h, C.byref(p), C.c_void_p(out_ptr), C.c_void_p(stream or None)))
 
+    def render_particles(self, settings: RenderSettings, count: int, first: int = 0) -> np.ndarray:
+        """Light-traced film ("adjoint_particle") of particles [first, first + count),
+        the whole film in ColorBuffer layout (x, y, rgb)."""
+        cam = self.scene.camera
+        out = np.zeros(cam.width * cam.height * 3, dtype=np.float32)
+        p = settings.to_c()
+        self._check(self.lib.rt_render_particles(self.h, C.byref(p), first, count, _ptr(out)))
+        return out.reshape(cam.width, cam.height, 3)
+
+    def render_particles_device(self, settings: RenderSettings, count: int, out_ptr: int, first: int = 0,
+                                stream: int = 0):
+        """Same, film written to device memory `out_ptr` (ScreenX*ScreenY*3 float32)."""
+        p = settings.to_c()
+        self._check(self.lib.rt_render_particles_device(self.h, C.byref(p), first, count, C.c_void_p(out_ptr),
+                                                        C.c_void_p(stream or None)))
+
+    def particle_splats(self, settings: RenderSettings, count: int, max_per: int, first: int = 0):
+        """Parity hook: each particle's camera connections, (n[count], pix[count, max_per],
+        rgb[count, max_per, 3]) with pix = x * ScreenY + y (-1 past n)."""
+        n = np.zeros(count, dtype=np.int32)
+        pix = np.zeros((count, max_per), dtype=np.int32)
+        rgb = np.zeros((count, max_per, 3), dtype=np.float32)
+        p = settings.to_c()
+        self._check(self.lib.rt_debug_particle_splats(self.h, C.byref(p), first, count, max_per, _ptr(n), _ptr(pix),
+                                                      _ptr(rgb)))
+        return n, pix, rgb
+
     def adjoint_forward(self, settings: RenderSettings) -> np.ndarray:
         """The film the gradients refer to (same as render)."""
         w, h = self._crop(settings)

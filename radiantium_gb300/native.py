@@ -9,7 +9,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 RT_OK = 0
 RT_ERR_INVALID_ARG = -1
@@ -26,7 +26,8 @@ FILTER_NEAREST, FILTER_LINEAR = 0, 1
 MAT_DIFFUSE, MAT_ROUGH_METAL, MAT_ROUGH_GLASS, MAT_ROUGH_PLASTIC, MAT_PERFECT_MIRROR, MAT_PERFECT_GLASS = range(6)
 DIST_BECKMANN, DIST_GGX = 0, 1
 GROUP_MESH, GROUP_SPHERE, GROUP_INSTANCE, GROUP_INFINITE_LIGHT = range(4)
-INTEGRATOR_PATH, INTEGRATOR_VOL_PATH = 0, 1
+INTEGRATOR_PATH, INTEGRATOR_VOL_PATH, INTEGRATOR_PARTICLE = 0, 1, 2
+PARTICLE_STREAM = 0x80000000
 METHOD_BXDF, METHOD_NEE, METHOD_MIS = 0, 1, 2
 STRATEGY_UNIFORM, STRATEGY_ALL = 0, 1
 HIT_TIE = 1
@@ -69,7 +70,8 @@ class GroupDesc(C.Structure):
 
 class CameraDesc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("near_z", C.c_float), ("far_z", C.c_float),
-                ("clip_to_camera", C.c_float * 16), ("camera_to_world", C.c_float * 16)]
+                ("clip_to_camera", C.c_float * 16), ("camera_to_world", C.c_float * 16),
+                ("camera_to_clip", C.c_float * 16), ("world_to_camera", C.c_float * 16)]
 
 
 class SceneDescC(C.Structure):
@@ -149,7 +151,7 @@ EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
     "rt_render", "rt_render_device", "rt_adjoint_forward", "rt_adjoint_backward", "rt_update_texture", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_autotune", "rt_get_stats", "rt_set_counting",
-    "rt_set_renderer", "rt_cancel",
+    "rt_set_renderer", "rt_cancel", "rt_render_particles", "rt_render_particles_device",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
 MAX_BATCH = 256
@@ -206,6 +208,12 @@ def _declare(lib):
     lib.rt_set_renderer.argtypes = [vp, C.c_int]
     lib.rt_cancel.restype = C.c_int
     lib.rt_cancel.argtypes = [vp]
+    lib.rt_render_particles.restype = C.c_int
+    lib.rt_render_particles.argtypes = [vp, C.POINTER(RenderParams), C.c_int64, C.c_int64, vp]
+    lib.rt_render_particles_device.restype = C.c_int
+    lib.rt_render_particles_device.argtypes = [vp, C.POINTER(RenderParams), C.c_int64, C.c_int64, vp, vp]
+    lib.rt_debug_particle_splats.restype = C.c_int
+    lib.rt_debug_particle_splats.argtypes = [vp, C.POINTER(RenderParams), C.c_int64, C.c_int64, C.c_int, vp, vp, vp]
     return lib
 
 

@@ -190,8 +190,8 @@ class Camera:
     def look_at(width, height, fov, origin, target, up=(0, 1, 0), near=0.001, far=1000.0):
         return Camera(width, height, fov, near, far, look_at_left_hand(origin, target, up))
 
-    def clip_to_camera(self) -> Mat4:
-        """Update(): inverse of perspective * translate * scale (Camera.cs:128-162)."""
+    def camera_to_clip(self) -> Mat4:
+        """Update(): perspective * translate * scale (Camera.cs:128-159)."""
         near, far = F(self.near), F(self.far)
         aspect = F(self.width) / F(self.height)
         recip = F(1) / (far - near)
@@ -201,8 +201,15 @@ class Camera:
         persp = Mat4([cot, 0, 0, 0, 0, cot, 0, 0, 0, 0, far * recip, 1, 0, 0, -near * far * recip, 0])
         scale = Mat4([F(-0.5), 0, 0, 0, 0, F(-0.5) * aspect, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1])
         trans = Mat4([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, -1, F(-1) / aspect, 0, 1])
-        p = (persp * trans) * scale
-        return p.invert()
+        return (persp * trans) * scale
+
+    def clip_to_camera(self) -> Mat4:
+        """Update(): Matrix4x4.Invert of camera->clip (Camera.cs:161-164)."""
+        return self.camera_to_clip().invert()
+
+    def world_to_camera(self) -> Mat4:
+        """Update(): Matrix4x4.Invert of camera->world (Camera.cs:166-170)."""
+        return self.camera_to_world.invert()
 
 
 # ---------------------------------------------------------------- scene tables ----
@@ -438,6 +445,8 @@ class PackedScene:
         d.camera.near_z, d.camera.far_z = cam.near, cam.far
         d.camera.clip_to_camera[:] = [float(v) for v in cam.clip_to_camera().m]
         d.camera.camera_to_world[:] = [float(v) for v in cam.camera_to_world.m]
+        d.camera.camera_to_clip[:] = [float(v) for v in cam.camera_to_clip().m]
+        d.camera.world_to_camera[:] = [float(v) for v in cam.world_to_camera().m]
         d.bvh_max_prims = s.bvh_max_prims
         self._keep = (keep, meshes, spheres, textures, mats, media, blas_groups, groups)
         self.desc = d

@@ -68,6 +68,15 @@ def hit_cases():
             ("instanced", inst, ((-6, 0, -6), (6, 3, 6)), 4)]
 
 
+def particle_cases():
+    """(name, scene, settings) of the light-tracer fixtures: per-particle splats of
+    particles [1000, 1512) and the film of particles [0, 20000) summed by one
+    oracle thread (a fixed order)."""
+    return [("cornell", *procedural.cornell_box(40, 30)),
+            ("zoo", *procedural.material_zoo(32, 32)),
+            ("instanced", *procedural.instanced_spheres(48, 32, sphere_n=12, grid=4, env_w=64, env_h=32))]
+
+
 def generate():
     out = {}
     rng = np.random.default_rng(2024)
@@ -102,6 +111,15 @@ def generate():
         orc = oracle.OracleScene(scene)
         film = orc.render(st)
         out[f"film_{name}"] = {"film": film.astype(np.float32).view(np.uint32)}
+        orc.close()
+    # light tracer (adjoint_particle)
+    for name, scene, st in particle_cases():
+        orc = oracle.OracleScene(scene)
+        pst = st.replace(integrator=N.INTEGRATOR_PARTICLE, seed=5)
+        n, pix, rgb = orc.particle_splats(pst, 512, 12, first=1000)
+        film = orc.render_particles(pst, 20000, threads=1)
+        out[f"particles_{name}"] = {"n": n, "pix": pix, "rgb": rgb.view(np.uint32),
+                                    "film": film.astype(np.float32).view(np.uint32)}
         orc.close()
     return out
 

@@ -30,7 +30,8 @@ def _bits(a):
 
 @pytest.mark.parametrize("name", ["philox", "detmath", "hits_cornell", "hits_instanced", "bvh_cornell",
                                   "film_cornell_bxdf", "film_cornell_nee", "film_cornell_mis",
-                                  "film_cornell_mis_all", "film_zoo_mis", "film_volume"])
+                                  "film_cornell_mis_all", "film_zoo_mis", "film_volume",
+                                  "particles_cornell", "particles_zoo", "particles_instanced"])
 def test_oracle_reproduces_golden(regenerated, name):
     want = _load(name)
     got = regenerated[name]
@@ -41,6 +42,10 @@ def test_oracle_reproduces_golden(regenerated, name):
 
 
 def test_golden_films_are_not_trivial():
-    for name in ["film_cornell_bxdf", "film_cornell_nee", "film_cornell_mis", "film_zoo_mis", "film_volume"]:
+    for name in ["film_cornell_bxdf", "film_cornell_nee", "film_cornell_mis", "film_zoo_mis", "film_volume",
+                 "particles_cornell", "particles_zoo", "particles_instanced"]:
         f = _load(name)["film"].view(np.float32)
         assert np.count_nonzero(f) > f.size // 4, name
+    for name in ["particles_cornell", "particles_zoo", "particles_instanced"]:
+        z = _load(name)
+        assert z["n"].sum() > 50 and (z["pix"] >= 0).sum() == np.minimum(z["n"], 12).sum(), name

@@ -275,3 +275,21 @@ def test_film_output_formats(tmp_path):
         RenderTarget = film
     paths = ResultOutput(True, False, True, str(tmp_path), "scene").save(R)
     assert [os.path.basename(p) for p in paths] == ["scene.png", "scene.exr"]
+
+
+def test_particle_tracer_agrees_with_path_tracer():
+    """The restated light tracer and path tracer estimate the same image: with
+    unbounded depth their mean radiance over the pixels that do not see the
+    light directly agree within 6% (the reference's splat mapping scales screen
+    positions by (ScreenX - 1, ScreenY - 1), which moves energy by about
+    (W / (W - 1)) * (H / (H - 1)) = 3% at 64 x 64; the rest is noise)."""
+    s, st = procedural.cornell_box(64, 64)
+    orc = O.OracleScene(s)
+    try:
+        img = orc.render_particles(st.replace(integrator=N.INTEGRATOR_PARTICLE, max_depth=-1, seed=3), 400000)
+        ref = orc.render(st.replace(spp=128, max_depth=-1, seed=4))
+    finally:
+        orc.close()
+    m = ref.max(axis=2) < 2
+    a, b = img[m].mean(axis=0), ref[m].mean(axis=0)
+    assert np.all(np.abs(a / b - 1) < 0.06), (a, b)
