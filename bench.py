@@ -864,9 +864,14 @@ def run_particles(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
+    from radiantium_gb300 import native as N
     scene, st = particle_workload()
     dev = Device(local)
     dev.upload(scene)
+    mode = {"auto": N.RENDERER_AUTO, "megakernel": N.RENDERER_MEGAKERNEL, "wavefront": N.RENDERER_WAVEFRONT,
+            "graph": N.RENDERER_WAVEFRONT_GRAPH}[args.renderer]
+    dev.set_renderer(mode)
+    wavefront = mode != N.RENDERER_MEGAKERNEL
     W, H = scene.camera.width, scene.camera.height
     per = args.particles_per_step
     base = rank * (args.warmup + 2 * args.steps + 1) * per    # disjoint particle ranges per rank
@@ -885,7 +890,7 @@ def run_particles(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    step_ms, kernel_ms, launches = [], 0.0, 0
+    step_ms, kernel_ms, shade_ms, launches, render_launches = [], 0.0, 0.0, 0, 0
     for i in range(args.steps):
         flush.fill_(float(i))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -896,7 +901,9 @@ def run_particles(args):
         step_ms.append(e0.elapsed_time(e1))
         s = dev.stats()
         kernel_ms += s["render_kernel_ms"]
+        shade_ms += s["shade_kernel_ms"]
         launches += s["kernel_launches"]
+        render_launches += s["render_launches"]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -924,11 +931,20 @@ def run_particles(args):
                 raise RuntimeError(dev.lib.rt_last_error(dev.h).decode())
         e2e = {"value": per * world / float(np.mean(times)), "unit": "particles/s", "h2d_bytes_per_step": 0,
                "d2h_bytes_per_step": W * H * 12, "note": "rt_render_particles with a pinned host film"}
-    # roofline of k_particles: algorithmic bytes from exact counts (the finishing
-    # pass's W*H camera rays are in the counts too; the splats' film atomics are not)
+    # roofline of the traversal kernels: algorithmic bytes from exact counts (the
+    # finishing pass's W*H camera rays are in the counts too; the splats' film
+    # atomics are not).  The graph-driven loop is timed as a whole, so the trace
+    # kernels' own time comes from one more (untimed) step of the host-driven loop.
     alg = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
            + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"])
-    kms = kernel_ms / args.steps
+    kms, sms, rls = kernel_ms / args.steps, shade_ms / args.steps, render_launches / args.steps
+    if wavefront and mode != N.RENDERER_WAVEFRONT:
+        dev.set_renderer(N.RENDERER_WAVEFRONT)
+        dev.render_particles_device(st, per, film.data_ptr(), first=base + (1 + args.warmup) * per, stream=stream)
+        torch.cuda.synchronize()
+        s = dev.stats()
+        kms, sms, rls = s["render_kernel_ms"], s["shade_kernel_ms"], s["render_launches"]
+        dev.set_renderer(mode)
     achieved = alg / (kms / 1000.0) / 1e9
     peak, peak_src = measured_peak()
     cpu = None
@@ -944,11 +960,18 @@ def run_particles(args):
         "data": "synthetic (seeded procedural scene)",
         "config": dict(particle_config(scene, st, per), parallelism=f"replicas x{world} (disjoint particle ranges)",
                        l2="256 MiB flush between timed steps (outside the CUDA events)",
-                       renderer="k_particles (one thread per particle) + k_particle_finish"),
+                       renderer=("wavefront (trace / shade kernels over compacted queues, particle regeneration)"
+                                 + (", bounce loop as a CUDA graph" if mode != N.RENDERER_WAVEFRONT else "")
+                                 if wavefront else "megakernel k_particles (one thread per particle)")
+                       + " + k_particle_finish"),
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_src, "kernel": "k_particles",
-                     "alg_bytes_per_step": alg, "kernel_ms_per_step": kms},
+                     "traffic": None, "peak_source": peak_src,
+                     "kernel": "k_wf_trace_closest + k_wf_trace_shadow" if wavefront else "k_particles",
+                     "alg_bytes_per_step": alg, "kernel_ms_per_step": kms,
+                     "launches_per_step": rls, "shade_ms_per_step": sms,
+                     "note": ("trace / shade times from one step of the host-driven loop"
+                              if wavefront and mode != N.RENDERER_WAVEFRONT else "")},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
                                                    "prim_tests", "instance_visits")},

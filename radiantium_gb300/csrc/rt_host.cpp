@@ -64,6 +64,7 @@ struct Ctx {
     int width = 0, height = 0;
     std::vector<RtTexture> h_textures;         /* host copies for the adjoint / texture updates */
     std::vector<RtMaterial> h_materials;
+    int mat_types = 0;                         /* distinct material types of the scene */
     std::vector<uint8_t> env_texture;          /* texture feeds an infinite light's sampling table */
     /* adjoint scratch */
     float* adj_dldi = nullptr; size_t adj_dldi_bytes = 0;
@@ -624,6 +625,11 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.textures = upload(c, texs);
     c->h_textures = texs;
     c->h_materials = mats;
+    {
+        uint32_t seen = 0;
+        for (const RtMaterial& m : mats) seen |= 1u << (m.type & 31);
+        c->mat_types = __builtin_popcount(seen);
+    }
     c->env_texture.assign(texs.size(), 0);
     for (int li : infinite) c->env_texture[lights[li].ref] = 1;
     v.texels = upload(c, texels);
@@ -780,6 +786,78 @@ RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64
     return P;
 }
 
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true);
+
+/* The light tracer as a wavefront (rt_wavefront.cu): one round over all the
+ * particles, path slots refilled with the next particle until none is left.
+ * The bounce loop is driven from the host or runs as one CUDA graph launch. */
+void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count, float* film, cudaStream_t s,
+                        bool use_graph) {
+    const int slots = (int)std::min<int64_t>(std::min<int64_t>(c->wf_capacity, WF_MAX_SLOTS), count + 31);
+    ensure_wf(c, slots);
+    ensure_events(c, 4);
+    CK(cudaStreamSynchronize(s));              /* the pinned staging is free */
+    WfJob& d = c->h_jobs[0];
+    d.view = c->d_view;
+    d.P = P;
+    d.samples = film;
+    d.first = first;
+    d.count = count;
+    CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(WfJob), cudaMemcpyHostToDevice, s));
+    WfState W = c->wf;
+    W.slots = slots;
+    W.shadow_base = 2 * slots;
+    W.refill = c->wf_refill;
+    std::memset(c->h_ctr, 0, sizeof(WfCounters));
+    c->h_ctr->total = count;
+    c->h_ctr->n_jobs = 1;
+    CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+    CK(rt_wf_start(W, s, true));
+    uint64_t launches = 2, trace_launches = 0;
+    double trace_ms = 0, shade_ms = 0;
+    const bool sort = c->mat_types > 1;
+    if (use_graph) {
+        ensure_wf_graph(c, W, false, true, sort);
+        CK(cudaEventRecord(c->events[0], s));
+        CK(cudaGraphLaunch(c->wf_exec, s));
+        CK(cudaEventRecord(c->events[1], s));
+        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
+        launches += (sort ? 7 : 5) * iters;
+        trace_launches += 2 * iters;
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
+        trace_ms += t;
+    } else {
+        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        /* a finished particle's last splat ray is still queued when its slot leaves the active list */
+        while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
+            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+            if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+            CK(cudaEventRecord(c->events[0], s));
+            CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+            CK(cudaEventRecord(c->events[1], s));
+            CK(cudaEventRecord(c->events[2], s));
+            CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false, s,
+                           &launches, WF_PASS_RENDER, nullptr, false, true, sort));
+            CK(cudaEventRecord(c->events[3], s));
+            launches += 2;
+            trace_launches += 2;
+            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
+            CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+        }
+    }
+    c->last.render_kernel_ms = trace_ms;
+    c->last.shade_kernel_ms = shade_ms;
+    c->last.render_launches = trace_launches;
+    c->last.kernel_launches = launches;
+}
+
 /* AdjointParticleRenderer (Renderers/AdjointParticleRenderer.cs:118-172): the
  * particles in launches of up to sample_budget, then the finishing pass */
 void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t count, float* dst, bool dst_host,
@@ -788,21 +866,30 @@ void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t 
     if (!dst) throw RtFail(RT_ERR_INVALID_ARG, "render_particles: null output");
     cudaStream_t s = user ? user : c->stream;
     const int64_t npix = (int64_t)P.w * P.h;
-    ensure(&c->film, &c->film_bytes, (size_t)npix * 12);
-    CK(cudaMemsetAsync(c->film, 0, (size_t)npix * 12, s));
+    ensure(&c->film, &c->film_bytes, (size_t)npix * 16);    /* float4 sums: one vector atomic per splat */
+    float4* film = reinterpret_cast<float4*>(c->film);
+    CK(cudaMemsetAsync(film, 0, (size_t)npix * 16, s));
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
+    const bool mega = c->renderer == RT_RENDERER_MEGAKERNEL;
     const int64_t chunk = std::max<int64_t>(1, c->sample_budget);
-    const int64_t nchunks = (count + chunk - 1) / chunk;
-    ensure_events(c, 2 * (size_t)nchunks);
-    for (int64_t b = 0, ci = 0; b < count; b += chunk, ci++) {
-        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-        CK(cudaEventRecord(c->events[2 * ci], s));
-        CK(rt_launch_particles(c->d_view, P, first + b, std::min(chunk, count - b), c->film, c->status, c->stats,
-                               c->counting, s));
-        CK(cudaEventRecord(c->events[2 * ci + 1], s));
+    const int64_t nchunks = mega ? (count + chunk - 1) / chunk : 0;
+    if (mega) {
+        ensure_events(c, 2 * (size_t)nchunks);
+        for (int64_t b = 0, ci = 0; b < count; b += chunk, ci++) {
+            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+            CK(cudaEventRecord(c->events[2 * ci], s));
+            CK(rt_launch_particles(c->d_view, P, first + b, std::min(chunk, count - b), film, c->status, c->stats,
+                                   c->counting, s));
+            CK(cudaEventRecord(c->events[2 * ci + 1], s));
+        }
+    } else {
+        /* AUTO: the graph-driven loop (the particles' long Russian-roulette tails make many short iterations) */
+        particle_wavefront(c, P, first, count, c->film, s,
+                           c->renderer == RT_RENDERER_WAVEFRONT_GRAPH || c->renderer == RT_RENDERER_AUTO);
     }
+    const rt_stats wf_last = c->last;
     float* out = dst;
     if (dst_host) {
         ensure(&c->out, &c->out_bytes, (size_t)npix * 12);
@@ -810,7 +897,7 @@ void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t 
     }
     /* float v = (float)ScreenX * ScreenY / pathCount (AdjointParticleRenderer.cs:156-157) */
     const float v = (float)P.w * (float)P.h / (float)count;
-    CK(rt_launch_particle_finish(c->d_view, npix, c->film, v, out, c->status, c->stats, c->counting, s));
+    CK(rt_launch_particle_finish(c->d_view, npix, film, v, out, c->status, c->stats, c->counting, s));
     if (dst_host) CK(cudaMemcpyAsync(dst, out, (size_t)npix * 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     check_status(c);
@@ -823,9 +910,16 @@ void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t 
     std::memset(&c->last, 0, sizeof(c->last));
     read_stats(c);
     c->last.samples = (uint64_t)count;
-    c->last.render_kernel_ms = ms;
-    c->last.render_launches = (uint64_t)nchunks;
-    c->last.kernel_launches = (uint64_t)nchunks + 1;
+    if (mega) {
+        c->last.render_kernel_ms = ms;
+        c->last.render_launches = (uint64_t)nchunks;
+        c->last.kernel_launches = (uint64_t)nchunks + 1;
+    } else {
+        c->last.render_kernel_ms = wf_last.render_kernel_ms;
+        c->last.shade_kernel_ms = wf_last.shade_kernel_ms;
+        c->last.render_launches = wf_last.render_launches;
+        c->last.kernel_launches = wf_last.kernel_launches + 1;
+    }
 }
 
 /* parity hook: each particle's camera connections into host arrays */
@@ -923,9 +1017,10 @@ struct WfJobIn {
  * (trace, phase, sort, shade, tail); the tail kernel clears the loop's
  * condition when no path is left.  Rebuilt when the path state moves or the
  * counting mode changes. */
-void ensure_wf_graph(Ctx* c, const WfState& W, bool vol) {
-    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 8) ^ ((uint64_t)W.refill << 2) ^
-                         ((uint64_t)vol << 1) ^ (c->counting ? 1u : 0u);
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sort) {
+    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 9) ^ ((uint64_t)sort << 8) ^
+                         ((uint64_t)particle << 7) ^ ((uint64_t)W.refill << 2) ^ ((uint64_t)vol << 1) ^
+                         (c->counting ? 1u : 0u);
     if (c->wf_exec && c->wf_graph_key == key) return;
     if (c->wf_exec) { cudaGraphExecDestroy(c->wf_exec); c->wf_exec = nullptr; }
     if (c->wf_graph) { cudaGraphDestroy(c->wf_graph); c->wf_graph = nullptr; }
@@ -944,7 +1039,7 @@ void ensure_wf_graph(Ctx* c, const WfState& W, bool vol) {
     uint64_t launches = 0;
     cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream);
     cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches,
-                                 WF_PASS_RENDER, nullptr, vol);
+                                 WF_PASS_RENDER, nullptr, vol, particle, sort);
     cudaGraph_t captured = nullptr;
     CK(cudaStreamEndCapture(c->stream, &captured));
     CK(e1);

@@ -24,14 +24,14 @@ cudaError_t rt_launch_adjoint(const RtSceneView* S, const RtParams& P, int albed
                               float* grad_albedo, float* grad_alpha, int n_alpha, const float* dLdI, uint32_t* status,
                               cudaStream_t stream);
 /* light tracing (rt_particles.cu): particles [first, first + count) splatted into
- * `film` sums; the record variant writes per-particle splat slots instead;
- * finish writes film * v + CameraTraceLight for every pixel */
-cudaError_t rt_launch_particles(const RtSceneView* S, const RtParams& P, int64_t first, int64_t count, float* film,
+ * `film` sums (one float4 per pixel); the record variant writes per-particle
+ * splat slots instead; finish writes film * v + CameraTraceLight for every pixel */
+cudaError_t rt_launch_particles(const RtSceneView* S, const RtParams& P, int64_t first, int64_t count, float4* film,
                                 uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
 cudaError_t rt_launch_particle_records(const RtSceneView* S, const RtParams& P, int64_t first, int64_t count,
                                        int32_t* rec_n, int32_t* rec_pix, float* rec_rgb, int rec_max,
                                        uint32_t* status, cudaStream_t stream);
-cudaError_t rt_launch_particle_finish(const RtSceneView* S, int64_t npix, const float* film, float v, float* out,
+cudaError_t rt_launch_particle_finish(const RtSceneView* S, int64_t npix, const float4* film, float v, float* out,
                                      uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
 cudaError_t rt_launch_scale(float* v, int64_t n, float s, cudaStream_t stream);
 cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream);

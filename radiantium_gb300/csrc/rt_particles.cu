@@ -33,7 +33,7 @@ DF void warp_add(unsigned long long* dst, uint32_t v) {
 
 /* where a particle's camera connections go: film sums, or per-particle records */
 struct SplatSink {
-    float* film;           /* ScreenX * ScreenY * 3 sums (ColorBuffer layout) */
+    float4* film;          /* ScreenX * ScreenY sums (ColorBuffer pixel order, one vector atomic per splat) */
     int32_t* rec_n;        /* records: splat count of each particle */
     int32_t* rec_pix;      /* x * ScreenY + y of its first rec_max splats */
     float* rec_rgb;
@@ -89,10 +89,7 @@ DF void EmitParticle(Ctx& c, const RtParams& P, int64_t i, int64_t slot, const S
                                 out.rec_rgb[3 * o + 2] = color.b;
                             }
                         } else if (x >= 0 && x < W && y >= 0 && y < H) {
-                            float* px = out.film + ((int64_t)x * H + y) * 3;
-                            atomicAdd(px, color.r);
-                            atomicAdd(px + 1, color.g);
-                            atomicAdd(px + 2, color.b);
+                            atomicAdd(out.film + ((int64_t)x * H + y), make_float4(color.r, color.g, color.b, 0.0f));
                         }
                         nsplat++;
                     }
@@ -137,7 +134,7 @@ __global__ void __launch_bounds__(128) k_particles(const RtSceneView* __restrict
 /* AdjointParticleRenderer.AfterRender (AdjointParticleRenderer.cs:156-172):
  * RefRGB(x, y) *= v, then += CameraTraceLight(camera.SampleRay((x, y)))
  * (AdjointParticleIntegrator.cs:81-84) */
-__global__ void __launch_bounds__(128) k_particle_finish(const RtSceneView* __restrict__ S, const float* __restrict__ film,
+__global__ void __launch_bounds__(128) k_particle_finish(const RtSceneView* __restrict__ S, const float4* __restrict__ film,
                                                            float v, float* __restrict__ out, uint32_t* status,
                                                            unsigned long long* stats, bool counting) {
     const int W = S->camera.width, H = S->camera.height;
@@ -150,7 +147,8 @@ __global__ void __launch_bounds__(128) k_particle_finish(const RtSceneView* __re
     const Ray ray = CameraRay(S->camera, v2((float)x, (float)y));
     Isect it;
     const C3 l = SceneIntersect(c, ray, &it) ? IsectLe(S, it, -ray.D) : EvalAllInfinite(S, ray.D);
-    C3 col = c3(film[3 * q], film[3 * q + 1], film[3 * q + 2]) * v;
+    const float4 sum = film[q];
+    C3 col = c3(sum.x, sum.y, sum.z) * v;
     col = col + l;
     out[3 * q] = col.r; out[3 * q + 1] = col.g; out[3 * q + 2] = col.b;
     if (counting) {
@@ -165,7 +163,7 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 }  // namespace
 
-cudaError_t rt_launch_particles(const RtSceneView* S, const RtParams& P, int64_t first, int64_t count, float* film,
+cudaError_t rt_launch_particles(const RtSceneView* S, const RtParams& P, int64_t first, int64_t count, float4* film,
                                 uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream) {
     if (count <= 0) return cudaSuccess;
     SplatSink out{film, nullptr, nullptr, nullptr, 0};
@@ -182,7 +180,7 @@ cudaError_t rt_launch_particle_records(const RtSceneView* S, const RtParams& P, 
     return cudaGetLastError();
 }
 
-cudaError_t rt_launch_particle_finish(const RtSceneView* S, int64_t npix, const float* film, float v, float* out,
+cudaError_t rt_launch_particle_finish(const RtSceneView* S, int64_t npix, const float4* film, float v, float* out,
                                      uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream) {
     k_particle_finish<<<grid_for(npix, 128), 128, 0, stream>>>(S, film, v, out, status, stats, counting);
     return cudaGetLastError();

@@ -227,6 +227,19 @@ __global__ void __launch_bounds__(128, 6) k_wf_trace_closest(WfState W, uint32_t
     }
 }
 
+/* a shadow ray's answer: the path's occlusion flag, or for a light-tracer
+ * camera connection its splat, added to the film sums when nothing is in the
+ * way (the reference's `lock (renderTarget)` add, AdjointParticleIntegrator.cs:53-66) */
+DF void shadow_done(const WfState& W, int meta, bool hit) {
+    const int path = meta_path(meta);
+    if (meta_kind(meta) != WF_RAY_SPLAT) { W.occluded[path] = hit ? 1 : 0; return; }
+    if (hit) return;
+    const float4 sp = W.pd_l1[path];
+    const int pix = __float_as_int(sp.w);
+    if (pix >= 0) atomicAdd(reinterpret_cast<float4*>(W.jobs[meta_job(meta)].samples) + pix,
+                            make_float4(sp.x, sp.y, sp.z, 0.0f));
+}
+
 /* shadow rays: any-hit (queue [shadow_base, shadow_base + n_shadow)) */
 __global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t* status, unsigned long long* stats,
                                                            bool counting) {
@@ -237,7 +250,7 @@ __global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t*
     uint32_t done = 0;
     TravAny T;
     const RtSceneView* S = nullptr;
-    int item = -1, path = 0;
+    int item = -1, meta = 0;
     bool exhausted = false;
     while (true) {
         const unsigned idle = __ballot_sync(kFullWarp, item < 0);
@@ -247,15 +260,14 @@ __global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t*
             const int e = fetch_entry(&W.ctr->fetch[1], n, idle, &exhausted);
             if (item < 0 && e < n) {
                 const int q = W.shadow_base + e;
-                const int meta = W.q_meta[q];
-                path = meta_path(meta);
+                meta = W.q_meta[q];
                 S = W.jobs[meta_job(meta)].view;
-                if (AnyBegin(S, queued_ray(W, q), T, pst)) { W.occluded[path] = 0; done++; }
+                if (AnyBegin(S, queued_ray(W, q), T, pst)) { shadow_done(W, meta, false); done++; }
                 else item = q;
             }
         }
         if (item >= 0 && AnyStep(S, T, stack, status, pst)) {
-            W.occluded[path] = T.hit ? 1 : 0;
+            shadow_done(W, meta, T.hit);
             done++;
             item = -1;
         }
@@ -967,6 +979,159 @@ __global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status
     }
 }
 
+/* ---- light tracing (AdjointParticleIntegrator.EmitParticle, AdjointParticleIntegrator.cs:24-79) ----
+ * A slot holds one particle; the job's `samples` is the film sums (float4 per
+ * pixel) and its `first` the index of the round's first particle.  The loop
+ * is cut at its two ray casts: the extension ray (Scene.Intersect) and the
+ * camera connection's shadow ray (Scene.IsOccluded), both traced in the next
+ * trace phase.  A shade runs one vertex: camera connection (its splat waits
+ * in pd_l1 and the shadow-ray kernel adds it when the way is clear),
+ * importance-mode BSDF sample, and the top of the reference's loop (depth
+ * limit, Russian roulette) before the next extension ray, so the random
+ * numbers are drawn in the reference's order.  A finished particle's slot
+ * takes the next particle at once: the new particle writes no splat before
+ * the pending shadow ray has been traced. */
+
+/* top of the bounce loop (AdjointParticleIntegrator.cs:34-42); false ends the particle */
+DF bool particle_continue(const RtParams& P, int bounces, C3* coeff, Rng& rand) {
+    if (P.max_depth != -1 && bounces >= P.max_depth) return false;
+    if (bounces > P.min_depth) {
+        if (NextFloat(rand) > P.rr) return false;
+        *coeff = *coeff / P.rr;
+    }
+    return true;
+}
+
+/* Claims particles for `slot` until one has an extension ray to trace (a
+ * particle can end before its first ray: no light, black emission, depth
+ * limit or roulette).  false once every particle of the round is claimed. */
+DF bool start_particle(const WfState& W, int slot) {
+    const WfJob& J = W.jobs[0];
+    const RtSceneView* S = J.view;
+    const RtParams P = J.P;
+    while (true) {
+        const long long sid = (long long)atomicAdd(&W.ctr->next_sample, 1ull);
+        if (sid >= W.ctr->total) { W.flags[slot] = 0; return false; }
+        const long long i = J.first + sid;
+        Rng rand;
+        rng_init(rand, P.seed, (uint32_t)(uint64_t)i, (uint32_t)((uint64_t)i >> 32), RT_PARTICLE_STREAM);
+        int light;
+        const float selectPdf = SampleLight(S, rand, &light);
+        if (selectPdf == 0.0f) continue;
+        const Emit e = LightSampleEmit(S, light, rand);
+        if (IsBlack(e.le)) continue;
+        C3 coeff = e.le * AbsDot(e.dir, e.n) / (selectPdf * e.pdf_pos * e.pdf_dir);
+        const Ray ray = mkray(e.pos, e.dir, 0.0001f);
+        if (!particle_continue(P, 1, &coeff, rand)) continue;
+        W.job[slot] = 0;
+        W.pix[slot] = make_int4((int)(uint32_t)(uint64_t)i, (int)(uint32_t)((uint64_t)i >> 32), 0, 0);
+        W.rng_n[slot] = rand.n;
+        W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.0f);
+        W.bounce[slot] = make_int2(1, 1);
+        W.flags[slot] = F_ALIVE | F_EXT;
+        W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
+        W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
+        const int q = warp_append(&W.ctr->n_closest, true);
+        push_ray(W, q, slot, WF_RAY_EXT, ray);
+        return true;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_wf_start_particles(WfState W) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= W.slots) return;
+    start_particle(W, slot);
+}
+
+DF void shade_particle(const WfState& W, int slot, int next, uint32_t* status) {
+    const WfJob& J = W.jobs[0];
+    const RtSceneView* S = J.view;
+    const RtParams P = J.P;
+    uint32_t fl = W.flags[slot];
+    bool done = (fl & F_DONE) != 0;
+    if (!done) {
+        /* 1. the vertex at the extension hit */
+        int2 bc = W.bounce[slot];
+        int bounces = bc.x, guard = bc.y;
+        const float4 cf = W.coeff[slot];
+        C3 coeff = c3(cf.x, cf.y, cf.z);
+        const float4 ro = W.ray_o[slot], rdd = W.ray_d[slot];
+        const Ray ray = mkray(v3(ro.x, ro.y, ro.z), v3(rdd.x, rdd.y, rdd.z), ro.w, rdd.w);
+        const int4 id = W.pix[slot];
+        Rng rand;
+        rng_resume(rand, P.seed, (uint32_t)id.x, (uint32_t)id.y, RT_PARTICLE_STREAM, W.rng_n[slot]);
+        Ray nray = ray;
+        bool ext = false;
+        do {
+            Isect it;
+            if (!load_hit(S, ray, W.ext_hit[slot], W.ext_sub[slot], &it)) { done = true; break; }
+            if (HasSurface(S, it)) {
+                const int mat = PrimOf(S, it).material;
+                const V3 wo = Lo(it, it.Wr);
+                CamWi cw;
+                if (CameraSampleWi(S->camera, it.P, &cw) && cw.we != 0.0f) {
+                    /* Scene.IsOccluded(camera, it.P): closer than 0.001 counts as occluded, no ray */
+                    const V3 vec = it.P - cw.pos;
+                    const float dis = Length(vec);
+                    if (!(dis < 0.001f)) {
+                        const V3 wi = Lo(it, cw.dir);
+                        const C3 f = MatFr<true>(S, mat, wo, wi, it.UV);
+                        const C3 color = coeff * f * cw.we * AbsCosTheta(wi);
+                        int pix = -1;   /* a NaN position (the reference throws) splats nothing */
+                        if (cw.sx == cw.sx && cw.sy == cw.sy) {
+                            const int x = (int)floorf(cw.sx), y = (int)floorf(cw.sy);
+                            if (x >= 0 && x < S->camera.width && y >= 0 && y < S->camera.height)
+                                pix = x * S->camera.height + y;
+                        }
+                        W.pd_l1[slot] = make_float4(color.r, color.g, color.b, __int_as_float(pix));
+                        const int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
+                        push_ray(W, q, slot, WF_RAY_SPLAT, mkray(cw.pos, Normalize(vec), 0.0001f, dis - 0.0001f));
+                    }
+                }
+                const BSample bs = MatSample<true>(S, mat, wo, it.UV, rand);
+                if (bs.Pdf > 0.0f) coeff = coeff * (bs.Fr * AbsCosTheta(bs.Wi) / bs.Pdf);
+                else { done = true; break; }
+                nray = Spawn(it, Wo(it, bs.Wi));
+                bounces++;
+            } else {
+                nray = mkray(it.P, ray.D, ray.MinT);   /* bounces-- and continue: the same depth again */
+            }
+            /* 2. the top of the next loop iteration */
+            if (++guard > RT_LOOP_CAP) { atomicOr(status, RT_STATUS_ITER); done = true; break; }
+            if (!particle_continue(P, bounces, &coeff, rand)) { done = true; break; }
+            ext = true;
+        } while (false);
+        if (ext) {
+            const int q = warp_append(&W.ctr->n_closest, true);
+            push_ray(W, q, slot, WF_RAY_EXT, nray);
+            W.ray_o[slot] = make_float4(nray.O.x, nray.O.y, nray.O.z, nray.MinT);
+            W.ray_d[slot] = make_float4(nray.D.x, nray.D.y, nray.D.z, nray.MaxT);
+        }
+        W.bounce[slot] = make_int2(bounces, guard);
+        W.rng_n[slot] = rand.n;
+        W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.0f);
+        if (done) fl |= F_DONE;
+    }
+    if (!(fl & F_DONE)) {
+        W.flags[slot] = fl;
+        const int a = warp_append(&W.ctr->n_active[next], true);
+        W.active[next][a] = slot;
+        return;
+    }
+    const bool more = start_particle(W, slot);
+    const int a = warp_append(&W.ctr->n_active[next], more);
+    if (more) W.active[next][a] = slot;
+}
+
+/* `sorted`: the list regrouped by shade key, else the active list as built
+ * (scenes of one material type gain nothing from the regrouping) */
+__global__ void __launch_bounds__(128, 6) k_wf_shade_particle(WfState W, uint32_t* status, bool sorted) {
+    const int cur = W.ctr->iter & 1;
+    const int n = min(W.ctr->n_active[cur], W.slots);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) shade_particle(W, sorted ? W.sorted[i] : W.active[cur][i], cur ^ 1, status);
+}
+
 __global__ void k_wf_active_init(WfState W) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= W.slots) return;
@@ -1051,7 +1216,9 @@ __global__ void k_wf_tail_loop(WfState W, cudaGraphConditionalHandle loop, uint3
     if (threadIdx.x == 0) {
         const int next = (W.ctr->iter & 1) ^ 1;
         W.ctr->iter++;
-        bool more = W.ctr->n_active[next] > 0;
+        /* queued shadow rays keep the loop going: a finished light-tracer
+         * particle leaves its last splat in the queue without an active slot */
+        bool more = W.ctr->n_active[next] > 0 || W.ctr->n_shadow > 0;
         if (more && W.ctr->iter >= WF_ITER_CAP) { atomicOr(status, RT_STATUS_ITER); more = false; }
         cudaGraphSetConditional(loop, more ? 1u : 0u);
     }
@@ -1071,8 +1238,9 @@ int resident_blocks(K kernel, int block) {
 
 }  // namespace
 
-cudaError_t rt_wf_start(const WfState& W, cudaStream_t s) {
-    k_wf_start<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
+cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle) {
+    if (particle) k_wf_start_particles<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
+    else k_wf_start<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_wf_active_init<<<grid_for(W.slots, 256), 256, 0, s>>>(W);
@@ -1091,7 +1259,7 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
 
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
                         cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
-                        int pass, const WfAdjoint* adj, bool vol) {
+                        int pass, const WfAdjoint* adj, bool vol, bool particle, bool sort) {
     static const int sort_blocks = resident_blocks(k_wf_sort_scatter, 256);
     static const int shade_blocks = resident_blocks(k_wf_shade<false, true>, 128);
     const WfAdjoint A = adj ? *adj : WfAdjoint{-1, 0, nullptr, nullptr, nullptr, nullptr};
@@ -1100,9 +1268,14 @@ cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned
     k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
     if (n > 0) {
         const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
-        k_wf_sort_count<<<sb, 256, 0, s>>>(W);
-        k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
-        if (vol) k_wf_shade_vol<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
+        if (sort || !particle) {
+            k_wf_sort_count<<<sb, 256, 0, s>>>(W);
+            k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
+        } else {
+            *launches -= 2;
+        }
+        if (particle) k_wf_shade_particle<<<grid_for(n, 128), 128, 0, s>>>(W, status, sort);
+        else if (vol) k_wf_shade_vol<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
         else if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A);
         else if (pass == WF_PASS_REPLAY) k_wf_shade<true, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
         else k_wf_shade<false, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);

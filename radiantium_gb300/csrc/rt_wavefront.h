@@ -17,15 +17,20 @@
 #include "rt_types.h"
 
 /* ray kinds: extension, shadow (any hit), MIS / IntersectTr-walk segment,
- * Transmittance-walk segment (the last three closest hit except shadow) */
+ * Transmittance-walk segment (the last three closest hit except shadow).
+ * In the shadow queue, WF_RAY_SPLAT marks a light-tracer camera connection:
+ * the trace kernel adds its pending splat to the film when the way is clear. */
 enum { WF_RAY_EXT = 0, WF_RAY_SHADOW = 1, WF_RAY_MIS = 2, WF_RAY_TRW = 3 };
+enum { WF_RAY_SPLAT = 2 };
 
 #define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
 #define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
 #define WF_SHADE_KEYS 16
 #define WF_ITER_CAP (1 << 20)      /* bounce iterations of one round before a run gives up */
 
-/* one render of a batch, for the current round of samples */
+/* one render of a batch, for the current round of samples (light tracing:
+ * `samples` is the film sums, one float4 per pixel, `first` the first
+ * particle index, `count` the particles of the round) */
 struct WfJob {
     const RtSceneView* view;       /* the job's scene (device) */
     RtParams P;                    /* chunk_begin / chunk_len: this round's sample indices */
@@ -86,7 +91,8 @@ struct WfState {
     float4* ray_o; float4* ray_d;
     /* direct-lighting term waiting for its shadow / MIS rays */
     float4* pd_coeff;        /* coeff at the bounce, light selection pdf */
-    float4* pd_l1;           /* light-sample term (NEE: the whole estimate) */
+    float4* pd_l1;           /* light-sample term (NEE: the whole estimate; light tracing:
+                                the splat's colour and film pixel) */
     float4* pd_fr;           /* BSDF-sample f*cos, MIS weight */
     float4* pd_mis;          /* BSDF pdf, light index */
     float4* pd_w;            /* direction passed to the light's L() */
@@ -110,18 +116,21 @@ struct WfState {
     float4* trw_hit; int32_t* trw_sub;
 };
 
-/* Starts the round: every slot takes a camera sample, the first active list
- * is built.  The counters must hold the round's total / n_jobs and zeros. */
-cudaError_t rt_wf_start(const WfState& W, cudaStream_t s);
+/* Starts the round: every slot takes a camera sample (or, `particle`, a light
+ * particle of job 0), the first active list is built.  The counters must hold
+ * the round's total / n_jobs and zeros. */
+cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false);
 /* Traces the queued closest-hit and shadow rays (lengths read on the device). */
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s);
-/* Shades the active paths, then advances the iteration; with `loop` set
+/* Shades the active paths (`particle`: light-tracer particles, regrouped by
+ * shade key only with `sort`), then advances the iteration; with `loop` set
  * (inside a captured while-loop), also sets the loop's condition to "paths
  * remain".  n_hint: the active count when the host knows it (grids sized to
  * it), -1 inside a graph (grids cover every slot, surplus blocks return).
  * Kernel launches are added to *launches. */
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,
                         cudaGraphConditionalHandle loop, bool has_loop, cudaStream_t s, uint64_t* launches,
-                        int pass = WF_PASS_RENDER, const WfAdjoint* adj = nullptr, bool vol = false);
+                        int pass = WF_PASS_RENDER, const WfAdjoint* adj = nullptr, bool vol = false,
+                        bool particle = false, bool sort = true);
 
 #endif

@@ -12,6 +12,8 @@ allow 1e-5 relative plus 1e-6 of the image maximum.  The finishing pass
 (scale by ScreenX * ScreenY / N plus CameraTraceLight) is the same arithmetic
 on both sides.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -33,6 +35,13 @@ SCENES = {
     "instanced": lambda: procedural.instanced_spheres(48, 32, sphere_n=12, grid=4, env_w=64, env_h=32),
     "volume": lambda: procedural.volume_box(32, 24),
 }
+
+
+def _set_limits(dev, sample_budget, capacity):
+    f = dev.lib.rt_debug_set_limits
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int64, C.c_int]
+    assert f(dev.h, sample_budget, capacity) == N.RT_OK
 
 
 def _film_close(got, want):
@@ -75,8 +84,13 @@ def test_particle_streams_above_2_32(dev):
                               b.view(np.uint32) if b.dtype == np.float32 else b)
 
 
-@pytest.mark.parametrize("name", ["cornell", "zoo", "instanced"])
+RENDERERS = [N.RENDERER_MEGAKERNEL, N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH]
+
+
+@pytest.mark.parametrize("name", ["cornell", "zoo", "instanced", "volume"])
 def test_film_matches_oracle(dev, name):
+    """Every renderer's film within the summation tolerance, and exactly the
+    oracle's ray, node, primitive and instance counts (the same rays traced)."""
     s, st = SCENES[name]()
     pst = _particle(st, seed=9)
     dev.upload(s)
@@ -85,17 +99,37 @@ def test_film_matches_oracle(dev, name):
         want, ost = orc.render_particles(pst, 200000, stats=True)
     finally:
         orc.close()
+    assert np.isfinite(want).all()
     dev.set_counting(True)
     try:
-        got = dev.render_particles(pst, 200000)
-        gst = dev.stats()
+        for mode in RENDERERS:
+            dev.set_renderer(mode)
+            got = dev.render_particles(pst, 200000)
+            gst = dev.stats()
+            assert _film_close(got, want) == 0, mode
+            assert gst["samples"] == 200000
+            for k in ("rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
+                assert gst[k] == ost[k], (mode, k)
     finally:
         dev.set_counting(False)
-    assert np.isfinite(want).all()
+        dev.set_renderer(N.RENDERER_AUTO)
+
+
+def test_wavefront_small_slot_pool(dev):
+    """Far more particles than path slots: slots are refilled until the range is done."""
+    s, st = SCENES["zoo"]()
+    pst = _particle(st, seed=13, max_depth=-1, min_depth=5)
+    dev.upload(s)
+    dev.set_renderer(N.RENDERER_MEGAKERNEL)
+    try:
+        want = dev.render_particles(pst, 50000).astype(np.float64)
+        dev.set_renderer(N.RENDERER_WAVEFRONT)
+        _set_limits(dev, 1 << 24, 1000)
+        got = dev.render_particles(pst, 50000)
+    finally:
+        _set_limits(dev, 1 << 24, N.MAX_SLOTS)
+        dev.set_renderer(N.RENDERER_AUTO)
     assert _film_close(got, want) == 0
-    assert gst["samples"] == 200000
-    for k in ("rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
-        assert gst[k] == ost[k], k
 
 
 def test_golden_particles(dev):
