@@ -9,9 +9,11 @@ entities like RendererBuilder.Build (RendererBuilder.cs:870-1010) and returns a
 :class:`GpuRenderer`, the drop-in replacement of BlockBasedRenderer: the
 renderer builders "block_based" and "gpu_wavefront" both create it.
 
-Plugins outside the GPU path (octree, bdpt, adjoint_particle, ao, gbuffer,
-disney, subsurface, image textures) raise NotImplementedError, the
-counterpart of the reference's NotSupportedException.
+The "adjoint_particle" integrator selects the light tracer
+(AdjointParticleRenderer, "particle_count"), rendered by the same class.
+Plugins outside the GPU path (octree, bdpt, ao, gbuffer, disney,
+subsurface, image files) raise NotImplementedError, the counterpart of the
+reference's NotSupportedException.
 """
 from __future__ import annotations
 

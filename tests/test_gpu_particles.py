@@ -187,3 +187,22 @@ def test_errors(dev):
     with pytest.raises(N.RTError) as e:
         dev.render(pst)
     assert e.value.code == N.RT_ERR_INVALID_ARG
+
+
+def test_scene_file_particle_renderer(tmp_path):
+    """A reference-schema scene file with the adjoint_particle integrator, rendered through
+    GpuRenderer (16 passes of particle ranges, count-weighted mean) against the oracle."""
+    from radiantium_gb300.config import load_scene_file
+    from tests.test_cpu_config import _scene_file
+    r = load_scene_file(_scene_file(tmp_path, {"type": "adjoint_particle", "min_depth": 4},
+                                    {"particle_count": 160000}))
+    r.Start()
+    r.Wait()
+    assert r.IsSuccess and r.CompletedTaskCount == 16
+    orc = oracle.OracleScene(r.scene)
+    try:
+        want = orc.render_particles(r.settings, 160000)
+    finally:
+        orc.close()
+    got = r.RenderTarget.astype(np.float64)
+    assert np.allclose(got, want, rtol=1e-4, atol=1e-5 * float(np.abs(want).max()))
