@@ -1011,6 +1011,7 @@ struct WfJobIn {
     const RtSceneView* view;
     RtParams P;
     float* film;
+    int mat_types;         /* distinct material types of the job's scene */
 };
 
 /* The bounce loop as a graph: a while node whose body is one iteration
@@ -1063,6 +1064,8 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         if ((J.P.integrator == RT_INTEGRATOR_VOL_PATH) != vol)
             throw RtFail(RT_ERR_UNSUPPORTED, "wavefront: a run renders one integrator");
     if (vol && adj) throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: the path integrator is differentiated");
+    /* the shade-key sort groups paths by material type: one scene of one type gains nothing from it */
+    const bool sort = jobs.size() > 1 || jobs[0].mat_types > 1;
     ensure_events(c, 4);
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
@@ -1112,14 +1115,14 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             CK(rt_wf_start(W, s));
             launches += 2;
             if (use_graph && pass == WF_PASS_RENDER) {
-                ensure_wf_graph(c, W, vol);
+                ensure_wf_graph(c, W, vol, false, sort);
                 CK(cudaEventRecord(c->events[0], s));
                 CK(cudaGraphLaunch(c->wf_exec, s));
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
                 CK(cudaStreamSynchronize(s));
                 const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
-                launches += 7 * iters;
+                launches += (sort ? 7 : 5) * iters;
                 trace_launches += 2 * iters;
                 float t = 0;
                 CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
@@ -1136,7 +1139,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaEventRecord(c->events[2], s));
                 CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
-                               s, &launches, pass, adj, vol));
+                               s, &launches, pass, adj, vol, false, sort));
                 CK(cudaEventRecord(c->events[3], s));
                 launches += 2;
                 trace_launches += 2;
@@ -1173,6 +1176,7 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     jobs[0].view = c->d_view;
     jobs[0].P = P;
     jobs[0].film = c->film;
+    jobs[0].mat_types = c->mat_types;
     wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH ||
                               (c->renderer == RT_RENDERER_AUTO && c->wf_graph_pref));
 }
@@ -1206,6 +1210,7 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
         P.spp = p->spp; P.sample_begin = p->sample_begin;
         jobs[i].view = sc->d_view;
         jobs[i].P = P;
+        jobs[i].mat_types = sc->mat_types;
         film_off[i] = film_floats;
         film_floats += (int64_t)P.w * P.h * 3;
     }
@@ -1304,6 +1309,7 @@ void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* 
         jobs[0].view = c->d_view;
         jobs[0].P = P;
         jobs[0].film = nullptr;
+        jobs[0].mat_types = c->mat_types;
         CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
         wavefront_run(c, jobs, s, false, &A);
         launches += c->last.kernel_launches;

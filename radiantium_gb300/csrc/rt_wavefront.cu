@@ -935,21 +935,23 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
 }
 
 __global__ void __launch_bounds__(128, 4) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
-                                                         bool counting) {
+                                                         bool counting, bool sorted) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) shade_vol_path(W, W.sorted[i], cur ^ 1, status, stats, counting);
+    if (i < n) shade_vol_path(W, sorted ? W.sorted[i] : W.active[cur][i], cur ^ 1, status, stats, counting);
 }
 
-/* the active paths of this iteration, one thread each over the sorted list:
- * either a grid sized to the active count, or (kDynamic, inside a graph where
- * the count is unknown at launch) a resident grid whose warps take the next
- * 32 entries from a counter until the list is done.  The replay pass of the
- * adjoint (kAdj) sums its alpha gradients per block in shared memory. */
+/* the active paths of this iteration, one thread each over the sorted list
+ * (or, `sorted` false, the active list as built): either a grid sized to the
+ * active count, or (kDynamic, inside a graph where the count is unknown at
+ * launch) a resident grid whose warps take the next 32 entries from a
+ * counter until the list is done.  The replay pass of the adjoint (kAdj)
+ * sums its alpha gradients per block in shared memory. */
 template <bool kAdj, bool kDynamic>
 __global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting,
-                                                       int pass, WfAdjoint A) {
+                                                       int pass, WfAdjoint A, bool sorted) {
+    const int32_t* list;
     __shared__ float s_alpha[kAdj ? RT_ADJ_MAX_ALPHA : 1];
     if (kAdj) {
         for (int i = threadIdx.x; i < A.n_alpha; i += blockDim.x) s_alpha[i] = 0.0f;
@@ -957,9 +959,10 @@ __global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status
     }
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
+    list = sorted ? W.sorted : W.active[cur];
     if (!kDynamic) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < n) shade_path<kAdj>(W, W.sorted[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+        if (i < n) shade_path<kAdj>(W, list[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
     } else {
         const int lane = threadIdx.x & 31;
         while (true) {
@@ -968,7 +971,7 @@ __global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status
             base = __shfl_sync(kFullWarp, base, 0);
             if (base >= n) break;
             const int i = base + lane;
-            if (i < n) shade_path<kAdj>(W, W.sorted[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+            if (i < n) shade_path<kAdj>(W, list[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
             __syncwarp();
         }
     }
@@ -1268,17 +1271,17 @@ cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned
     k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
     if (n > 0) {
         const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
-        if (sort || !particle) {
+        if (sort) {
             k_wf_sort_count<<<sb, 256, 0, s>>>(W);
             k_wf_sort_scatter<<<sb, 256, 0, s>>>(W);
         } else {
             *launches -= 2;
         }
         if (particle) k_wf_shade_particle<<<grid_for(n, 128), 128, 0, s>>>(W, status, sort);
-        else if (vol) k_wf_shade_vol<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting);
-        else if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A);
-        else if (pass == WF_PASS_REPLAY) k_wf_shade<true, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
-        else k_wf_shade<false, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A);
+        else if (vol) k_wf_shade_vol<<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, sort);
+        else if (!known) k_wf_shade<false, true><<<shade_blocks, 128, 0, s>>>(W, status, stats, counting, pass, A, sort);
+        else if (pass == WF_PASS_REPLAY) k_wf_shade<true, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A, sort);
+        else k_wf_shade<false, false><<<grid_for(n, 128), 128, 0, s>>>(W, status, stats, counting, pass, A, sort);
         *launches += 3;
     }
     if (has_loop) k_wf_tail_loop<<<1, 32, 0, s>>>(W, loop, status);

@@ -122,8 +122,8 @@ struct WfState {
 cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false);
 /* Traces the queued closest-hit and shadow rays (lengths read on the device). */
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s);
-/* Shades the active paths (`particle`: light-tracer particles, regrouped by
- * shade key only with `sort`), then advances the iteration; with `loop` set
+/* Shades the active paths (`particle`: light-tracer particles) - regrouped by
+ * shade key first with `sort` - then advances the iteration; with `loop` set
  * (inside a captured while-loop), also sets the loop's condition to "paths
  * remain".  n_hint: the active count when the host knows it (grids sized to
  * it), -1 inside a graph (grids cover every slot, surplus blocks return).
