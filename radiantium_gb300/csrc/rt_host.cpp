@@ -788,69 +788,79 @@ RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64
 
 void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true);
 
-/* The light tracer as a wavefront (rt_wavefront.cu): one round over all the
- * particles, path slots refilled with the next particle until none is left.
- * The bounce loop is driven from the host or runs as one CUDA graph launch. */
+/* The light tracer as a wavefront (rt_wavefront.cu): rounds of up to
+ * 4 x sample_budget particles (cancellation is checked between rounds); in
+ * a round, path slots are refilled with the next particle until none is
+ * left.  The bounce loop is driven from the host or runs as one CUDA graph
+ * launch per round. */
 void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count, float* film, cudaStream_t s,
                         bool use_graph) {
-    const int slots = (int)std::min<int64_t>(std::min<int64_t>(c->wf_capacity, WF_MAX_SLOTS), count + 31);
+    const int64_t round_max = std::max<int64_t>(1, 4 * c->sample_budget);
+    const int slots = (int)std::min<int64_t>(std::min<int64_t>(c->wf_capacity, WF_MAX_SLOTS),
+                                             std::min(count, round_max) + 31);
     ensure_wf(c, slots);
     ensure_events(c, 4);
-    CK(cudaStreamSynchronize(s));              /* the pinned staging is free */
-    WfJob& d = c->h_jobs[0];
-    d.view = c->d_view;
-    d.P = P;
-    d.samples = film;
-    d.first = first;
-    d.count = count;
-    CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(WfJob), cudaMemcpyHostToDevice, s));
     WfState W = c->wf;
     W.slots = slots;
     W.shadow_base = 2 * slots;
     W.refill = c->wf_refill;
-    std::memset(c->h_ctr, 0, sizeof(WfCounters));
-    c->h_ctr->total = count;
-    c->h_ctr->n_jobs = 1;
-    CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
-    CK(rt_wf_start(W, s, true));
-    uint64_t launches = 2, trace_launches = 0;
-    double trace_ms = 0, shade_ms = 0;
     const bool sort = c->mat_types > 1;
-    if (use_graph) {
-        ensure_wf_graph(c, W, false, true, sort);
-        CK(cudaEventRecord(c->events[0], s));
-        CK(cudaGraphLaunch(c->wf_exec, s));
-        CK(cudaEventRecord(c->events[1], s));
-        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
-        launches += (sort ? 7 : 5) * iters;
-        trace_launches += 2 * iters;
-        float t = 0;
-        CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
-        trace_ms += t;
-    } else {
-        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        /* a finished particle's last splat ray is still queued when its slot leaves the active list */
-        while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
-            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-            if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+    uint64_t launches = 0, trace_launches = 0;
+    double trace_ms = 0, shade_ms = 0;
+    for (int64_t done = 0; done < count;) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        const int64_t n = std::min(round_max, count - done);
+        CK(cudaStreamSynchronize(s));          /* the pinned staging is free */
+        WfJob& d = c->h_jobs[0];
+        d.view = c->d_view;
+        d.P = P;
+        d.samples = film;
+        d.first = first + done;
+        d.count = n;
+        CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(WfJob), cudaMemcpyHostToDevice, s));
+        std::memset(c->h_ctr, 0, sizeof(WfCounters));
+        c->h_ctr->total = n;
+        c->h_ctr->n_jobs = 1;
+        CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+        CK(rt_wf_start(W, s, true));
+        launches += 2;
+        if (use_graph) {
+            ensure_wf_graph(c, W, false, true, sort);
             CK(cudaEventRecord(c->events[0], s));
-            CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+            CK(cudaGraphLaunch(c->wf_exec, s));
             CK(cudaEventRecord(c->events[1], s));
-            CK(cudaEventRecord(c->events[2], s));
-            CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false, s,
-                           &launches, WF_PASS_RENDER, nullptr, false, true, sort));
-            CK(cudaEventRecord(c->events[3], s));
-            launches += 2;
-            trace_launches += 2;
             CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
+            const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
+            launches += (sort ? 7 : 5) * iters;
+            trace_launches += 2 * iters;
             float t = 0;
-            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
-            CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
+            trace_ms += t;                     /* the whole loop: not split by phase */
+        } else {
+            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            /* a finished particle's last splat ray is still queued when its slot leaves the active list */
+            while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
+                if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+                if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+                CK(cudaEventRecord(c->events[0], s));
+                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+                CK(cudaEventRecord(c->events[1], s));
+                CK(cudaEventRecord(c->events[2], s));
+                CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
+                               s, &launches, WF_PASS_RENDER, nullptr, false, true, sort));
+                CK(cudaEventRecord(c->events[3], s));
+                launches += 2;
+                trace_launches += 2;
+                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                float t = 0;
+                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
+                CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
+            }
         }
+        done += n;
     }
     c->last.render_kernel_ms = trace_ms;
     c->last.shade_kernel_ms = shade_ms;

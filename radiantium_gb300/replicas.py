@@ -6,6 +6,11 @@ same film (`sample_begin`), and the films are combined once at the end: the
 spp-weighted sum of the rank films, reduced over the ranks, divided by the
 total spp (BlockBasedRenderer's per-pixel average).  The combined film
 equals the one-GPU film up to the order of the final float additions.
+
+The light tracer shards the same way over particle ranges: particle i's
+random numbers depend only on (seed, i), and each rank's film is already its
+splats scaled by 1/(its particle count) plus CameraTraceLight, so the
+count-weighted mean of the rank films is the film of all the particles.
 """
 from __future__ import annotations
 
@@ -42,3 +47,16 @@ def render_replicated(render, settings, rank: int, world: int, group=None) -> np
         probe = render(settings.replace(spp=1))
         film = np.zeros_like(probe)
     return combine(film, count, settings.spp, group)
+
+
+def render_particles_replicated(render_particles, settings, count: int, rank: int, world: int,
+                                group=None) -> np.ndarray:
+    """render_particles(settings, n, first) -> film of particles [first, first + n) (the
+    light tracer, "adjoint_particle"); returns the film of particles [0, count)."""
+    if count < 1:
+        raise ValueError("particle count must be >= 1")
+    first, n = sample_range(rank, world, count)
+    film = render_particles(settings, n, first) if n > 0 else None
+    if film is None:
+        film = np.zeros_like(render_particles(settings, 1, 0))
+    return combine(film, n, count, group)

@@ -132,6 +132,25 @@ def test_wavefront_small_slot_pool(dev):
     assert _film_close(got, want) == 0
 
 
+@pytest.mark.parametrize("mode", [N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH])
+def test_wavefront_rounds(dev, mode):
+    """A particle range longer than one round (4 x the sample budget) renders in
+    rounds; the film is the same as the megakernel's."""
+    s, st = SCENES["instanced"]()
+    pst = _particle(st, seed=17)
+    dev.upload(s)
+    dev.set_renderer(N.RENDERER_MEGAKERNEL)
+    try:
+        want = dev.render_particles(pst, 30000, first=77).astype(np.float64)
+        dev.set_renderer(mode)
+        _set_limits(dev, 1000, 0)          # rounds of 4000 particles
+        got = dev.render_particles(pst, 30000, first=77)
+    finally:
+        _set_limits(dev, 1 << 24, 0)
+        dev.set_renderer(N.RENDERER_AUTO)
+    assert _film_close(got, want) == 0
+
+
 def test_golden_particles(dev):
     """Against the committed fixtures (made by the oracle; this test reads them as files)."""
     import os
