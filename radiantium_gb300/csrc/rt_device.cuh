@@ -410,6 +410,28 @@ DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
     return h.root_ref;
 }
 
+/* Traversal stack storage: a thread-local array, or (SplitStack) the first
+ * RT_SH_STACK entries in shared memory - one column of a block-wide array per
+ * thread, so a warp's accesses fall in distinct banks - and the rest in the
+ * thread's local array.  Both levels share one index range (the prototype's
+ * entries start where the top level's end), so the shared entries hold the
+ * bottom of the combined stack. */
+#ifndef RT_SH_STACK
+#define RT_SH_STACK 16
+#endif
+#define RT_TRACE_BLOCK 128            /* threads per block of the kernels that use SplitStack */
+struct SplitStack {
+    int2* sh;                         /* &block_array[threadIdx.x]; entry i at sh[i * RT_TRACE_BLOCK] */
+    int2* loc;                        /* 2 * RT_STACK_SIZE entries */
+};
+DF int2 stk_get(int2* s, int i) { return s[i]; }
+DF void stk_put(int2* s, int i, int2 v) { s[i] = v; }
+DF int2 stk_get(const SplitStack& s, int i) { return i < RT_SH_STACK ? s.sh[i * RT_TRACE_BLOCK] : s.loc[i]; }
+DF void stk_put(const SplitStack& s, int i, int2 v) {
+    if (i < RT_SH_STACK) s.sh[i * RT_TRACE_BLOCK] = v;
+    else s.loc[i] = v;
+}
+
 /* One interior node: both child boxes are read from the parent, the far child
  * is pushed with its entry distance and re-checked against the MaxT current
  * when it is popped, which is exactly when the reference tests it.  A far
@@ -419,7 +441,8 @@ DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
  * never pops, nor counts, what is left on its stack) and for trees tall
  * enough to overflow the stack.  Returns the near child to descend into, or
  * RT_NO_NODE. */
-DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int* sp, TravStats* st) {
+template <class Stk>
+DF int VisitNode(const RtSceneView* S, int node, const Ray& r, Stk stack, int* sp, TravStats* st) {
     const float4* np = S->nodes + 4 * (int64_t)node;
     const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3);
     const int lref = __float_as_int(n3.x), rref = __float_as_int(n3.y), axis = __float_as_int(n3.z);
@@ -431,14 +454,16 @@ DF int VisitNode(const RtSceneView* S, int node, const Ray& r, int2* stack, int*
     const int nearRef = rightFirst ? rref : lref, farRef = rightFirst ? lref : rref;
     const bool nearA = rightFirst ? ar : al, farA = rightFirst ? al : ar;
     const float nearT = rightFirst ? tr : tl, farT = rightFirst ? tl : tr;
-    if (farA || st || S->deep_trees) stack[(*sp)++] = make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000)));
+    if (farA || st || S->deep_trees)
+        stk_put(stack, (*sp)++, make_int2(farRef, __float_as_int(farA ? farT : __int_as_float(0x7fc00000))));
     return (nearA && nearT < r.MaxT) ? nearRef : RT_NO_NODE;
 }
 
 /* Pops until an entry passes the MaxT check (Bvh.cs:205-229 / 153-169). */
-DF int PopNext(int2* stack, int* sp, int base, float maxT, TravStats* st) {
+template <class Stk>
+DF int PopNext(Stk stack, int* sp, int base, float maxT, TravStats* st) {
     while (*sp > base) {
-        const int2 e = stack[--*sp];
+        const int2 e = stk_get(stack, --*sp);
         if (st) st->nodes++;
         if (__int_as_float(e.y) < maxT) return e.x;
     }
@@ -492,7 +517,8 @@ DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravS
 }
 
 /* One step; true when the traversal has finished. */
-DF bool ClosestStep(const RtSceneView* S, TravClosest& T, int2* stack, uint32_t* status, TravStats* st) {
+template <class Stk>
+DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
     if (T.leafLeft > 0) {
         const int slot = T.leafSlot++;
@@ -639,7 +665,8 @@ DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st
 }
 
 /* One step; true when the traversal has finished (T.hit holds the answer). */
-DF bool AnyStep(const RtSceneView* S, TravAny& T, int2* stack, uint32_t* status, TravStats* st) {
+template <class Stk>
+DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
     if (T.leafLeft > 0) {
         const int slot = T.leafSlot++;

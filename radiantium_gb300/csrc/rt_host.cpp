@@ -65,6 +65,7 @@ struct Ctx {
     std::vector<RtTexture> h_textures;         /* host copies for the adjoint / texture updates */
     std::vector<RtMaterial> h_materials;
     int mat_types = 0;                         /* distinct material types of the scene */
+    int tallest = 0;                           /* levels of the scene's tallest tree */
     std::vector<uint8_t> env_texture;          /* texture feeds an infinite light's sampling table */
     /* adjoint scratch */
     float* adj_dldi = nullptr; size_t adj_dldi_bytes = 0;
@@ -642,6 +643,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.infinite_count = (int)infinite.size();
     v.global_medium = d->global_medium < 0 ? -1 : d->global_medium;
     v.deep_trees = tallest > RT_STACK_SIZE + 1 ? 1 : 0;
+    c->tallest = tallest;
     RtCamera& cam = v.camera;
     cam.width = d->camera.width; cam.height = d->camera.height;
     cam.near_z = d->camera.near_z; cam.far_z = d->camera.far_z;
@@ -786,7 +788,7 @@ RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64
     return P;
 }
 
-void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true);
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true, bool deep = false);
 
 /* The light tracer as a wavefront (rt_wavefront.cu): rounds of up to
  * 4 x sample_budget particles (cancellation is checked between rounds); in
@@ -804,7 +806,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
     W.slots = slots;
     W.shadow_base = 2 * slots;
     W.refill = c->wf_refill;
-    const bool sort = c->mat_types > 1;
+    const bool sort = c->mat_types > 1, deep = c->tallest >= RT_DEEP_TREE;
     uint64_t launches = 0, trace_launches = 0;
     double trace_ms = 0, shade_ms = 0;
     for (int64_t done = 0; done < count;) {
@@ -825,7 +827,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
         CK(rt_wf_start(W, s, true));
         launches += 2;
         if (use_graph) {
-            ensure_wf_graph(c, W, false, true, sort);
+            ensure_wf_graph(c, W, false, true, sort, deep);
             CK(cudaEventRecord(c->events[0], s));
             CK(cudaGraphLaunch(c->wf_exec, s));
             CK(cudaEventRecord(c->events[1], s));
@@ -845,7 +847,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
                 if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
                 if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
                 CK(cudaEventRecord(c->events[0], s));
-                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaEventRecord(c->events[2], s));
                 CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
@@ -1022,16 +1024,17 @@ struct WfJobIn {
     RtParams P;
     float* film;
     int mat_types;         /* distinct material types of the job's scene */
+    int tallest;           /* levels of its tallest tree */
 };
 
 /* The bounce loop as a graph: a while node whose body is one iteration
  * (trace, phase, sort, shade, tail); the tail kernel clears the loop's
  * condition when no path is left.  Rebuilt when the path state moves or the
  * counting mode changes. */
-void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sort) {
-    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 9) ^ ((uint64_t)sort << 8) ^
-                         ((uint64_t)particle << 7) ^ ((uint64_t)W.refill << 2) ^ ((uint64_t)vol << 1) ^
-                         (c->counting ? 1u : 0u);
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sort, bool deep) {
+    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 10) ^ ((uint64_t)deep << 9) ^
+                         ((uint64_t)sort << 8) ^ ((uint64_t)particle << 7) ^ ((uint64_t)W.refill << 2) ^
+                         ((uint64_t)vol << 1) ^ (c->counting ? 1u : 0u);
     if (c->wf_exec && c->wf_graph_key == key) return;
     if (c->wf_exec) { cudaGraphExecDestroy(c->wf_exec); c->wf_exec = nullptr; }
     if (c->wf_graph) { cudaGraphDestroy(c->wf_graph); c->wf_graph = nullptr; }
@@ -1048,7 +1051,7 @@ void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sor
     cudaGraph_t body = np.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     uint64_t launches = 0;
-    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream);
+    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream, deep);
     cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches,
                                  WF_PASS_RENDER, nullptr, vol, particle, sort);
     cudaGraph_t captured = nullptr;
@@ -1076,6 +1079,8 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
     if (vol && adj) throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: the path integrator is differentiated");
     /* the shade-key sort groups paths by material type: one scene of one type gains nothing from it */
     const bool sort = jobs.size() > 1 || jobs[0].mat_types > 1;
+    bool deep = false;
+    for (const WfJobIn& J : jobs) deep = deep || J.tallest >= RT_DEEP_TREE;
     ensure_events(c, 4);
     double trace_ms = 0, shade_ms = 0;
     uint64_t launches = 0, trace_launches = 0;
@@ -1125,7 +1130,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             CK(rt_wf_start(W, s));
             launches += 2;
             if (use_graph && pass == WF_PASS_RENDER) {
-                ensure_wf_graph(c, W, vol, false, sort);
+                ensure_wf_graph(c, W, vol, false, sort, deep);
                 CK(cudaEventRecord(c->events[0], s));
                 CK(cudaGraphLaunch(c->wf_exec, s));
                 CK(cudaEventRecord(c->events[1], s));
@@ -1145,7 +1150,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
                 if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
                 if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
                 CK(cudaEventRecord(c->events[0], s));
-                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s));
+                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
                 CK(cudaEventRecord(c->events[1], s));
                 CK(cudaEventRecord(c->events[2], s));
                 CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
@@ -1187,6 +1192,7 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     jobs[0].P = P;
     jobs[0].film = c->film;
     jobs[0].mat_types = c->mat_types;
+    jobs[0].tallest = c->tallest;
     wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH ||
                               (c->renderer == RT_RENDERER_AUTO && c->wf_graph_pref));
 }
@@ -1221,6 +1227,7 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
         jobs[i].view = sc->d_view;
         jobs[i].P = P;
         jobs[i].mat_types = sc->mat_types;
+        jobs[i].tallest = sc->tallest;
         film_off[i] = film_floats;
         film_floats += (int64_t)P.w * P.h * 3;
     }
@@ -1320,6 +1327,7 @@ void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* 
         jobs[0].P = P;
         jobs[0].film = nullptr;
         jobs[0].mat_types = c->mat_types;
+        jobs[0].tallest = c->tallest;
         CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
         wavefront_run(c, jobs, s, false, &A);
         launches += c->last.kernel_launches;

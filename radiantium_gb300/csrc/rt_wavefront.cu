@@ -167,6 +167,15 @@ __global__ void __launch_bounds__(256) k_wf_start(WfState W) {
  * and the per-ray results are the same as a one-ray-per-thread launch. */
 constexpr unsigned kFullWarp = 0xffffffffu;
 
+/* resident blocks of 128 threads per SM the trace kernels are compiled for
+ * (the register budget: 65536 / (128 * blocks)) */
+#ifndef RT_CLOSEST_BLOCKS
+#define RT_CLOSEST_BLOCKS 6
+#endif
+#ifndef RT_SHADOW_BLOCKS
+#define RT_SHADOW_BLOCKS 7
+#endif
+
 /* One warp-wide fetch: returns this lane's queue entry (>= n: none) and sets
  * `exhausted` (warp-uniform) once the queue has been handed out. */
 DF int fetch_entry(int32_t* counter, int n, unsigned idle, bool* exhausted) {
@@ -192,11 +201,30 @@ DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
     else { W.trw_hit[path] = h; W.trw_sub[path] = T.best.sub; }
 }
 
+/* The traversal stack of a trace kernel: with kSh (scenes with tall trees)
+ * its bottom RT_SH_STACK entries live in shared memory, which keeps the stack
+ * of a deep traversal out of the L1 lines the node data needs; shallow trees
+ * keep the whole stack in local memory, where it stays in a few hot lines. */
+template <bool kSh> struct TraceStack;
+template <> struct TraceStack<false> {
+    int2 a[2 * RT_STACK_SIZE];
+    DF int2* get() { return a; }
+};
+template <> struct TraceStack<true> {
+    int2 a[2 * RT_STACK_SIZE];
+    DF SplitStack get() {
+        __shared__ int2 sh[RT_SH_STACK * RT_TRACE_BLOCK];
+        return SplitStack{sh + threadIdx.x, a};
+    }
+};
+
 /* closest-hit rays: extension and MIS rays (queue [0, n_closest)) */
-__global__ void __launch_bounds__(128, 6) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
+template <bool kSh>
+__global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_CLOSEST_BLOCKS) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
                                                             bool counting) {
     const int n = min(W.ctr->n_closest, 2 * W.slots);
-    int2 stack[2 * RT_STACK_SIZE];
+    TraceStack<kSh> stk;
+    const auto stack = stk.get();
     TravStats st = {0, 0, 0};
     TravStats* pst = counting ? &st : nullptr;
     uint32_t done = 0;
@@ -241,10 +269,12 @@ DF void shadow_done(const WfState& W, int meta, bool hit) {
 }
 
 /* shadow rays: any-hit (queue [shadow_base, shadow_base + n_shadow)) */
-__global__ void __launch_bounds__(128, 7) k_wf_trace_shadow(WfState W, uint32_t* status, unsigned long long* stats,
+template <bool kSh>
+__global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_SHADOW_BLOCKS) k_wf_trace_shadow(WfState W, uint32_t* status, unsigned long long* stats,
                                                            bool counting) {
     const int n = min(W.ctr->n_shadow, W.slots);
-    int2 stack[2 * RT_STACK_SIZE];
+    TraceStack<kSh> stk;
+    const auto stack = stk.get();
     TravStats st = {0, 0, 0};
     TravStats* pst = counting ? &st : nullptr;
     uint32_t done = 0;
@@ -1250,13 +1280,18 @@ cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle) {
     return cudaGetLastError();
 }
 
-cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s) {
-    static const int closest_blocks = resident_blocks(k_wf_trace_closest, 128);
-    static const int shadow_blocks = resident_blocks(k_wf_trace_shadow, 128);
-    k_wf_trace_closest<<<closest_blocks, 128, 0, s>>>(W, status, stats, counting);
+cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
+                        bool deep) {
+    static const int closest_blocks[2] = {resident_blocks(k_wf_trace_closest<false>, RT_TRACE_BLOCK),
+                                          resident_blocks(k_wf_trace_closest<true>, RT_TRACE_BLOCK)};
+    static const int shadow_blocks[2] = {resident_blocks(k_wf_trace_shadow<false>, RT_TRACE_BLOCK),
+                                         resident_blocks(k_wf_trace_shadow<true>, RT_TRACE_BLOCK)};
+    if (deep) k_wf_trace_closest<true><<<closest_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
+    else k_wf_trace_closest<false><<<closest_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_wf_trace_shadow<<<shadow_blocks, 128, 0, s>>>(W, status, stats, counting);
+    if (deep) k_wf_trace_shadow<true><<<shadow_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
+    else k_wf_trace_shadow<false><<<shadow_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
     return cudaGetLastError();
 }
 

@@ -120,8 +120,12 @@ struct WfState {
  * particle of job 0), the first active list is built.  The counters must hold
  * the round's total / n_jobs and zeros. */
 cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false);
-/* Traces the queued closest-hit and shadow rays (lengths read on the device). */
-cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s);
+/* Traces the queued closest-hit and shadow rays (lengths read on the device);
+ * `deep`: a tree of the scene has RT_DEEP_TREE levels or more, the kernels
+ * keep the bottom of the traversal stack in shared memory. */
+#define RT_DEEP_TREE 16
+cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
+                        bool deep = false);
 /* Shades the active paths (`particle`: light-tracer particles) - regrouped by
  * shade key first with `sort` - then advances the iteration; with `loop` set
  * (inside a captured while-loop), also sets the loop's condition to "paths

@@ -165,6 +165,30 @@ def test_wavefront_matches_megakernel_large(dev):
     assert np.array_equal(_bits(b[20:44, 30:46]), _bits(o))
 
 
+def test_wavefront_tall_tree_matches_megakernel(dev):
+    """A prototype of 12 * 64^2 = 49,152 triangles (one per leaf) has a tree of at
+    least 17 levels, so the wavefront's trace kernels keep the bottom of their
+    stacks in shared memory (trees of RT_DEEP_TREE = 16 levels or more): films and
+    traversal counters equal the megakernel's for the host- and graph-driven loops."""
+    from radiantium_gb300 import procedural as P
+    s, st = P.instanced_spheres(64, 48, sphere_n=64, grid=2, env_w=64, env_h=32)
+    dev.upload(s)
+    st = st.replace(spp=8)
+    dev.set_counting(True)
+    try:
+        a = _render(dev, st, N.RENDERER_MEGAKERNEL)
+        ca = dev.stats()
+        for mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH):
+            b = _render(dev, st, mode)
+            cb = dev.stats()
+            assert np.array_equal(_bits(a), _bits(b)), (mode, float(np.abs(a - b).max()))
+            if mode == N.RENDERER_WAVEFRONT:
+                for k in ("samples", "rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
+                    assert ca[k] == cb[k], (k, ca[k], cb[k])
+    finally:
+        dev.set_counting(False)
+
+
 @pytest.mark.parametrize("renderer", RENDERERS)
 def test_render_volume_bitexact(dev, renderer):
     """vol_path: the megakernel for both light strategies, the wavefront (with its

@@ -151,6 +151,29 @@ def test_wavefront_rounds(dev, mode):
     assert _film_close(got, want) == 0
 
 
+def test_tall_tree_wavefront_matches_megakernel(dev):
+    """A 49,152-triangle prototype (trees of 17+ levels: the shared-memory stack
+    trace kernels): the wavefront traces the megakernel's rays and node visits."""
+    s, st = procedural.instanced_spheres(48, 32, sphere_n=64, grid=2, env_w=64, env_h=32)
+    pst = _particle(st, seed=23)
+    dev.upload(s)
+    dev.set_counting(True)
+    try:
+        dev.set_renderer(N.RENDERER_MEGAKERNEL)
+        want = dev.render_particles(pst, 100000).astype(np.float64)
+        cw = dev.stats()
+        for mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH):
+            dev.set_renderer(mode)
+            got = dev.render_particles(pst, 100000)
+            cg = dev.stats()
+            assert _film_close(got, want) == 0, mode
+            for k in ("rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
+                assert cg[k] == cw[k], (mode, k)
+    finally:
+        dev.set_counting(False)
+        dev.set_renderer(N.RENDERER_AUTO)
+
+
 def test_golden_particles(dev):
     """Against the committed fixtures (made by the oracle; this test reads them as files)."""
     import os
