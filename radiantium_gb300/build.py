@@ -35,7 +35,7 @@ def _cuda_home():
     raise RuntimeError("nvcc not found")
 
 
-def build(verbose: bool = False, extra_nvcc=()) -> str:
+def build(verbose: bool = False, extra_nvcc=(), extra_cxx=()) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OUT_DIR, exist_ok=True)
@@ -52,7 +52,7 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
                          *extra_nvcc, "-c", os.path.join(CSRC, "rt_bvh_gpu.cu")],
         "rt_noalloc.o": [nvcc, ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *extra_nvcc,
                          "-c", os.path.join(CSRC, "rt_noalloc.cu")],
-        "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+        "rt_host.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", *extra_cxx,
                       f"-I{cuda}/include", "-c", os.path.join(CSRC, "rt_host.cpp")],
         "rt_bvh.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                      "-c", os.path.join(CSRC, "rt_bvh.cpp")],

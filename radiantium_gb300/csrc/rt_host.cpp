@@ -1077,8 +1077,9 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         if ((J.P.integrator == RT_INTEGRATOR_VOL_PATH) != vol)
             throw RtFail(RT_ERR_UNSUPPORTED, "wavefront: a run renders one integrator");
     if (vol && adj) throw RtFail(RT_ERR_UNSUPPORTED, "adjoint: the path integrator is differentiated");
-    /* the shade-key sort groups paths by material type: one scene of one type gains nothing from it */
-    const bool sort = jobs.size() > 1 || jobs[0].mat_types > 1;
+    /* the shade-key sort groups paths by material type: one `path` scene of one type gains nothing
+     * from it; vol_path keys also separate medium-boundary hits and paths advancing boundary walks */
+    const bool sort = vol || jobs.size() > 1 || jobs[0].mat_types > 1;
     bool deep = false;
     for (const WfJobIn& J : jobs) deep = deep || J.tallest >= RT_DEEP_TREE;
     ensure_events(c, 4);

@@ -123,7 +123,9 @@ cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false)
 /* Traces the queued closest-hit and shadow rays (lengths read on the device);
  * `deep`: a tree of the scene has RT_DEEP_TREE levels or more, the kernels
  * keep the bottom of the traversal stack in shared memory. */
+#ifndef RT_DEEP_TREE
 #define RT_DEEP_TREE 16
+#endif
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
                         bool deep = false);
 /* Shades the active paths (`particle`: light-tracer particles) - regrouped by
