@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
     ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
     ap.add_argument("--no-relmse", action="store_true", help="skip the converged render for relMSE")
+    ap.add_argument("--autotune", choices=["on", "off"], default="off",
+                    help="path workloads: pick the wavefront settings with rt_autotune on one step (untimed); "
+                         "off by default: the defaults were as fast on C1-C3, and a 1-spp probe picked settings "
+                         "that lose on full steps")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="steps of the plain megakernel timed in the same run for the batched/plain ratio (0: skip)")
     return ap.parse_args()
@@ -256,6 +260,14 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
 
+    # untimed, optional: the film-preserving wavefront settings (slots in flight, trace-warp
+    # refill, host- or graph-driven loop) picked by rt_autotune on one step of this workload
+    tuned = None
+    if uses_wavefront and mode == N.RENDERER_AUTO and args.autotune == "on":
+        tuned = dev.autotune([(dev, st.replace(spp=spp_step, sample_begin=base))])
+    graph_loop = mode == N.RENDERER_WAVEFRONT_GRAPH or (tuned is not None and
+                                                         tuned["renderer"] == N.RENDERER_WAVEFRONT_GRAPH)
+
     # one untimed counting pass: exact traversal counts of this workload
     dev.set_counting(True)
     dev.render_device(st.replace(spp=spp_step, sample_begin=base), film.data_ptr(), stream)
@@ -353,9 +365,19 @@ def run_ours(args):
         plain = {"value": samples_step / (float(np.mean(pt)) / 1000.0), "unit": "samples/s", "steps": args.plain_steps,
                  "note": "plain megakernel (one thread per camera sample), same passes, identical films"}
 
-    # roofline of the path-tracing kernel (algorithmic bytes from exact counts)
+    # roofline of the path-tracing kernel (algorithmic bytes from exact counts); a
+    # graph-driven loop is timed as a whole, so the trace kernels' own time then
+    # comes from one more (untimed) step of the host-driven loop
     alg_bytes_step = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
                       + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"] + B_FILM * counts["samples"])
+    if graph_loop:
+        dev.set_renderer(N.RENDERER_WAVEFRONT)
+        dev.render_device(st.replace(spp=spp_step, sample_begin=base + args.warmup * spp_step), film.data_ptr(), stream)
+        torch.cuda.synchronize()
+        s = dev.stats()
+        kernel_ms, shade_ms = s["render_kernel_ms"] * args.steps, s["shade_kernel_ms"] * args.steps
+        render_launches = s["render_launches"] * args.steps
+        dev.set_renderer(mode)
     # wavefront: every traversal launch of a step together traces the step's rays,
     # so the roofline uses the step's algorithmic bytes over its summed traversal time
     launches_per_step = max(1, render_launches // args.steps)
@@ -376,7 +398,9 @@ def run_ours(args):
                        parallelism=f"replicas x{world} (independent sample passes)",
                        l2="256 MiB flush between timed steps (outside the CUDA events)",
                        renderer=("wavefront (trace / shade kernels over compacted queues, path regeneration)"
-                                 if uses_wavefront else "plain megakernel (one thread per camera sample)")),
+                                 + (", bounce loop as a CUDA graph" if graph_loop else "")
+                                 if uses_wavefront else "plain megakernel (one thread per camera sample)"),
+                       autotune=tuned),
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
