@@ -175,6 +175,18 @@ constexpr unsigned kFullWarp = 0xffffffffu;
 #ifndef RT_SHADOW_BLOCKS
 #define RT_SHADOW_BLOCKS 7
 #endif
+/* the same for the shade kernels of `path` (the host-driven render pass; the
+ * graph-driven and adjoint-replay variants keep 5, where 6 spills far more)
+ * and of the light tracer */
+#ifndef RT_SHADE_BLOCKS
+#define RT_SHADE_BLOCKS 6
+#endif
+#ifndef RT_PSHADE_BLOCKS
+#define RT_PSHADE_BLOCKS 6
+#endif
+#ifndef RT_VSHADE_BLOCKS
+#define RT_VSHADE_BLOCKS 4
+#endif
 
 /* One warp-wide fetch: returns this lane's queue entry (>= n: none) and sets
  * `exhausted` (warp-uniform) once the queue has been handed out. */
@@ -964,7 +976,7 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
     }
 }
 
-__global__ void __launch_bounds__(128, 4) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
+__global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
                                                          bool counting, bool sorted) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
@@ -979,7 +991,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade_vol(WfState W, uint32_t* st
  * counter until the list is done.  The replay pass of the adjoint (kAdj)
  * sums its alpha gradients per block in shared memory. */
 template <bool kAdj, bool kDynamic>
-__global__ void __launch_bounds__(128, 5) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting,
+__global__ void __launch_bounds__(128, (kAdj || kDynamic) ? 5 : RT_SHADE_BLOCKS) k_wf_shade(WfState W, uint32_t* status, unsigned long long* stats, bool counting,
                                                        int pass, WfAdjoint A, bool sorted) {
     const int32_t* list;
     __shared__ float s_alpha[kAdj ? RT_ADJ_MAX_ALPHA : 1];
@@ -1158,7 +1170,7 @@ DF void shade_particle(const WfState& W, int slot, int next, uint32_t* status) {
 
 /* `sorted`: the list regrouped by shade key, else the active list as built
  * (scenes of one material type gain nothing from the regrouping) */
-__global__ void __launch_bounds__(128, 6) k_wf_shade_particle(WfState W, uint32_t* status, bool sorted) {
+__global__ void __launch_bounds__(128, RT_PSHADE_BLOCKS) k_wf_shade_particle(WfState W, uint32_t* status, bool sorted) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
