@@ -265,8 +265,9 @@ def run_ours(args):
     tuned = None
     if uses_wavefront and mode == N.RENDERER_AUTO and args.autotune == "on":
         tuned = dev.autotune([(dev, st.replace(spp=spp_step, sample_begin=base))])
-    graph_loop = mode == N.RENDERER_WAVEFRONT_GRAPH or (tuned is not None and
-                                                         tuned["renderer"] == N.RENDERER_WAVEFRONT_GRAPH)
+    # the library's AUTO rule: vol_path (and an autotune that picked it) runs the graph-driven loop
+    graph_loop = mode == N.RENDERER_WAVEFRONT_GRAPH or (mode == N.RENDERER_AUTO and (
+        st.integrator == N.INTEGRATOR_VOL_PATH or (tuned is not None and tuned["renderer"] == N.RENDERER_WAVEFRONT_GRAPH)))
 
     # one untimed counting pass: exact traversal counts of this workload
     dev.set_counting(True)

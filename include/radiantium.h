@@ -341,8 +341,8 @@ int rt_set_counting(void* ctx, int enabled);
 
 /* Selects the render pipeline: RT_RENDERER_AUTO (wavefront where it applies,
  * i.e. the `path` and `vol_path` integrators with the Uniform light
- * strategy, megakernel otherwise; the light tracer runs its wavefront as a
- * CUDA graph), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
+ * strategy, megakernel otherwise; vol_path and the light tracer drive their
+ * wavefront loop as a CUDA graph), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
  * driven by the host, with per-phase timings in rt_stats) or
  * RT_RENDERER_WAVEFRONT_GRAPH (bounce loop as one CUDA graph launch per
  * round of samples).  All produce identical camera-path films (light-tracer

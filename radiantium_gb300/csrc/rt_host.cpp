@@ -1196,8 +1196,11 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     jobs[0].film = c->film;
     jobs[0].mat_types = c->mat_types;
     jobs[0].tallest = c->tallest;
+    /* AUTO drives vol_path's loop as a graph: its boundary walks make ~100 short iterations per
+     * round, where the host loop's per-iteration synchronisation costs 9 % (C3) */
+    const bool vol = P.integrator == RT_INTEGRATOR_VOL_PATH;
     wavefront_run(c, jobs, s, c->renderer == RT_RENDERER_WAVEFRONT_GRAPH ||
-                              (c->renderer == RT_RENDERER_AUTO && c->wf_graph_pref));
+                              (c->renderer == RT_RENDERER_AUTO && (c->wf_graph_pref || vol)));
 }
 
 /* rt_render_batch(_device): every item's film through one wavefront run;
