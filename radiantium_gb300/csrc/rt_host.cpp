@@ -32,9 +32,19 @@
 #include "rt_bvh_gpu.h"
 #include "rt_launch.h"
 #include "rt_types.h"
+#include <nvtx3/nvToolsExt.h>
 #include "rt_wavefront.h"
 
 namespace {
+
+/* NVTX range over a scope: calls and wavefront phases show up named in
+ * Nsight timelines; without a tool attached a push/pop is a no-op call */
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct RtFail : std::runtime_error {
     int code;
@@ -364,6 +374,7 @@ rtb::Box xform_box(const rtb::Box& b, const float* m) {
 }
 
 void upload_scene(Ctx* c, const rt_scene_desc* d) {
+    NvtxRange nvtx_("rt.upload_scene");
     if (!d || d->abi_version != RT_ABI_VERSION) throw RtFail(RT_ERR_INVALID_ARG, "scene: null descriptor or ABI version mismatch");
     if (d->camera.width <= 0 || d->camera.height <= 0) throw RtFail(RT_ERR_INVALID_ARG, "scene: camera resolution must be positive");
     const int threads = std::max(1u, std::thread::hardware_concurrency());
@@ -694,6 +705,7 @@ void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t
 void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s);
 
 void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaStream_t user) {
+    NvtxRange nvtx_("rt.render");
     if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
     if (!p || !dst || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render: null params/output or spp <= 0");
     if (p->integrator != RT_INTEGRATOR_PATH && p->integrator != RT_INTEGRATOR_VOL_PATH) throw RtFail(RT_ERR_INVALID_ARG, "render: unknown integrator");
@@ -846,6 +858,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
             while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
                 if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
                 if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+                NvtxRange nvtx_iter("rt.wavefront_iteration");
                 CK(cudaEventRecord(c->events[0], s));
                 CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
                 CK(cudaEventRecord(c->events[1], s));
@@ -874,6 +887,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
  * particles in launches of up to sample_budget, then the finishing pass */
 void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t count, float* dst, bool dst_host,
                       cudaStream_t user) {
+    NvtxRange nvtx_("rt.render_particles");
     RtParams P = particle_params(c, p, first, count);
     if (!dst) throw RtFail(RT_ERR_INVALID_ARG, "render_particles: null output");
     cudaStream_t s = user ? user : c->stream;
@@ -1152,6 +1166,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0) {
                 if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
                 if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+                NvtxRange nvtx_iter("rt.wavefront_iteration");
                 CK(cudaEventRecord(c->events[0], s));
                 CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
                 CK(cudaEventRecord(c->events[1], s));
@@ -1206,6 +1221,7 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
 /* rt_render_batch(_device): every item's film through one wavefront run;
  * out_rgb are host pointers, or device pointers written on `user` */
 void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cudaStream_t user) {
+    NvtxRange nvtx_("rt.render_batch");
     if (!items || n <= 0 || n > WF_MAX_JOBS) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: 1 to 256 items");
     std::vector<WfJobIn> jobs((size_t)n);
     std::vector<int64_t> film_off((size_t)n);
@@ -1275,6 +1291,7 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
  * (rt_adjoint.cu), chunked over samples like the megakernel render */
 void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* d, const float* dldi, float* g_albedo,
                       float* g_alpha) {
+    NvtxRange nvtx_("rt.adjoint_backward");
     if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
     if (!p || !d || !dldi || p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "adjoint: null params / descriptor / dL_dimage or spp <= 0");
     if (p->integrator != RT_INTEGRATOR_PATH || p->method != RT_METHOD_MIS)
@@ -1378,6 +1395,7 @@ void update_texture(Ctx* c, int tex, const float* texels) {
  * unchanged (path slots in flight, trace-warp refill threshold, host- or
  * graph-driven bounce loop) and keeps the fastest on the context */
 void autotune(Ctx* c, const rt_batch_item* items, int n, rt_tune_result* out) {
+    NvtxRange nvtx_("rt.autotune");
     if (!items || n <= 0 || !out) throw RtFail(RT_ERR_INVALID_ARG, "autotune: no items or no result");
     const int caps[] = {WF_MAX_SLOTS, WF_MAX_SLOTS / 2, WF_MAX_SLOTS / 4};
     const int refills[] = {8, 4, 16};
@@ -1412,6 +1430,7 @@ void autotune(Ctx* c, const rt_batch_item* items, int n, rt_tune_result* out) {
 }
 
 void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bool host, cudaStream_t user) {
+    NvtxRange nvtx_("rt.trace");
     if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
     if (n < 0 || (n > 0 && (!rays || (!hits && !occ)))) throw RtFail(RT_ERR_INVALID_ARG, "trace: bad arguments");
     cudaStream_t s = user ? user : c->stream;
