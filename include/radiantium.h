@@ -47,6 +47,7 @@ extern "C" {
 #define RT_ERR_NO_SCENE (-6)
 #define RT_ERR_UNSUPPORTED (-7)
 #define RT_ERR_STACK (-8)      /* BVH traversal stack (64 entries, Bvh.cs:16) overflowed */
+#define RT_ERR_BOUNDS (-9)     /* debug-bounds builds only: a device index left its buffer */
 
 /* ---- enums (values mirror the reference enums) -------------------------- */
 #define RT_WRAP_CLAMP 0        /* TextureSampler.cs:5-9 WrapMode */

@@ -35,10 +35,14 @@ def _cuda_home():
     raise RuntimeError("nvcc not found")
 
 
-def build(verbose: bool = False, extra_nvcc=(), extra_cxx=()) -> str:
+def build(verbose: bool = False, extra_nvcc=(), extra_cxx=(), out_dir: str = OUT_DIR) -> str:
+    """Compiles every translation unit in parallel and links the library into
+    `out_dir`; returns the library's path.  A variant build (for example the
+    debug-bounds one, extra_nvcc=["-DRT_DEBUG_BOUNDS"]) goes to its own out_dir."""
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    os.makedirs(OUT_DIR, exist_ok=True)
+    os.makedirs(out_dir, exist_ok=True)
+    lib = os.path.join(out_dir, os.path.basename(LIB))
     objs = {
         "rt_kernels.o": [nvcc, ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-warn-spills", *extra_nvcc, "-c", os.path.join(CSRC, "rt_kernels.cu")],
@@ -59,7 +63,7 @@ def build(verbose: bool = False, extra_nvcc=(), extra_cxx=()) -> str:
     }
     procs = []
     for obj, cmd in objs.items():
-        full = cmd + ["-o", os.path.join(OUT_DIR, obj)]
+        full = cmd + ["-o", os.path.join(out_dir, obj)]
         if verbose:
             print(" ".join(full))
         procs.append((obj, subprocess.Popen(full, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
@@ -72,9 +76,9 @@ def build(verbose: bool = False, extra_nvcc=(), extra_cxx=()) -> str:
             failed.append(obj)
     if failed:
         raise RuntimeError(f"radiantium_gb300 build failed: {failed}")
-    link = [nvcc, ARCH, "-shared", "-o", LIB] + [os.path.join(OUT_DIR, o) for o in objs] + ["-lpthread"]
+    link = [nvcc, ARCH, "-shared", "-o", lib] + [os.path.join(out_dir, o) for o in objs] + ["-lpthread"]
     subprocess.run(link, check=True)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

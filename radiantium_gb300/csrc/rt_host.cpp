@@ -202,6 +202,7 @@ void ensure_wf(Ctx* c, int slots) {
     if (!c->h_jobs) CK(cudaMallocHost((void**)&c->h_jobs, WF_MAX_JOBS * sizeof(WfJob)));
     W.ctr = c->d_ctr;
     W.jobs = c->d_jobs;
+    W.status = c->status;
     c->wf_slots = slots;
     c->wf_generation++;
 }
@@ -691,6 +692,7 @@ void check_status(Ctx* c) {
     if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
     if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
     if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
+    if (st & RT_STATUS_BOUNDS) throw RtFail(RT_ERR_BOUNDS, "a device index left its buffer (debug-bounds build)");
 }
 
 void read_stats(Ctx* c) {
@@ -1030,6 +1032,7 @@ void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t 
     if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
     if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
     if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
+    if (st & RT_STATUS_BOUNDS) throw RtFail(RT_ERR_BOUNDS, "a device index left its buffer (debug-bounds build)");
 }
 
 /* one render of a wavefront run: scene, parameters (full spp), film sums */

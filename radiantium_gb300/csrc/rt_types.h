@@ -32,6 +32,7 @@
 #define RT_STATUS_STACK 1u
 #define RT_STATUS_ITER 2u
 #define RT_STATUS_BADREF 4u
+#define RT_STATUS_BOUNDS 8u         /* debug-bounds builds: an index left its buffer, the access was skipped */
 
 #define RT_LIGHT_AREA_TRI 0
 #define RT_LIGHT_AREA_SPHERE 1

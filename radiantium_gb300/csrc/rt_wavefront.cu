@@ -72,7 +72,24 @@ DF int warp_append(int* counter, bool want) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+/* Debug-bounds builds (-DRT_DEBUG_BOUNDS) check every computed index into a
+ * path-state buffer: one outside its buffer sets RT_STATUS_BOUNDS and the
+ * access is skipped (no trap), so the host reports RT_ERR_BOUNDS. */
+#ifdef RT_DEBUG_BOUNDS
+DF bool in_bounds(const WfState& W, long long i, long long n) {
+    if (i >= 0 && i < n) return true;
+    atomicOr(W.status, RT_STATUS_BOUNDS);
+    return false;
+}
+#else
+DF bool in_bounds(const WfState&, long long, long long) { return true; }
+#endif
+DF void set_active(const WfState& W, int list, int a, int slot) {
+    if (in_bounds(W, a, W.slots)) W.active[list][a] = slot;
+}
+
 DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
+    if (!in_bounds(W, q, 3LL * W.slots)) return;
     W.q_o[q] = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
     W.q_d[q] = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
     W.q_meta[q] = (path << 10) | ((int)W.job[path] << 2) | kind;
@@ -276,8 +293,9 @@ DF void shadow_done(const WfState& W, int meta, bool hit) {
     if (hit) return;
     const float4 sp = W.pd_l1[path];
     const int pix = __float_as_int(sp.w);
-    if (pix >= 0) atomicAdd(reinterpret_cast<float4*>(W.jobs[meta_job(meta)].samples) + pix,
-                            make_float4(sp.x, sp.y, sp.z, 0.0f));
+    const WfJob& J = W.jobs[meta_job(meta)];
+    if (pix >= 0 && in_bounds(W, pix, (long long)J.P.w * J.P.h))
+        atomicAdd(reinterpret_cast<float4*>(J.samples) + pix, make_float4(sp.x, sp.y, sp.z, 0.0f));
 }
 
 /* shadow rays: any-hit (queue [shadow_base, shadow_base + n_shadow)) */
@@ -364,7 +382,9 @@ DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned
     int4 px = W.pix[slot];
     const RtParams& P = J.P;
     const int64_t npix = (int64_t)P.w * P.h;
-    float* o = J.samples + ((int64_t)px.z * npix + (int64_t)px.x * P.h + px.y) * 3;
+    const int64_t sample = (int64_t)px.z * npix + (int64_t)px.x * P.h + px.y;
+    if (!in_bounds(W, sample, J.count)) return;
+    float* o = J.samples + sample * 3;
     o[0] = rad.r; o[1] = rad.g; o[2] = rad.b;
 }
 
@@ -610,14 +630,14 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
     if ((fl & F_PENDING) || !(fl & F_DONE)) {
         W.flags[slot] = fl;
         int a = warp_append(&W.ctr->n_active[next], true);
-        W.active[next][a] = slot;
+        set_active(W, next, a, slot);
         return;
     }
     finish_path(J, W, slot, radiance, stats, pass);
     if (counting) warp_add64(stats + 0, 1u);
     if (start_path(W, slot, true)) {
         int a = warp_append(&W.ctr->n_active[next], true);
-        W.active[next][a] = slot;
+        set_active(W, next, a, slot);
     } else {
         W.flags[slot] = 0;
         warp_append(&W.ctr->n_active[next], false);
@@ -740,7 +760,7 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
         if (fl & (F_WTR | F_WIT)) {
             W.flags[slot] = fl;
             const int a = warp_append(&W.ctr->n_active[next], true);
-            W.active[next][a] = slot;
+            set_active(W, next, a, slot);
             return;
         }
     }
@@ -961,7 +981,7 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
     if (ext || (fl & (F_WTR | F_WIT))) {
         W.flags[slot] = fl;
         const int a = warp_append(&W.ctr->n_active[next], true);
-        W.active[next][a] = slot;
+        set_active(W, next, a, slot);
         return;
     }
     /* the path is over */
@@ -969,7 +989,7 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
     if (counting) warp_add64(stats + 0, 1u);
     if (start_path(W, slot, true)) {
         const int a = warp_append(&W.ctr->n_active[next], true);
-        W.active[next][a] = slot;
+        set_active(W, next, a, slot);
     } else {
         W.flags[slot] = 0;
         warp_append(&W.ctr->n_active[next], false);
@@ -1160,12 +1180,12 @@ DF void shade_particle(const WfState& W, int slot, int next, uint32_t* status) {
     if (!(fl & F_DONE)) {
         W.flags[slot] = fl;
         const int a = warp_append(&W.ctr->n_active[next], true);
-        W.active[next][a] = slot;
+        set_active(W, next, a, slot);
         return;
     }
     const bool more = start_particle(W, slot);
     const int a = warp_append(&W.ctr->n_active[next], more);
-    if (more) W.active[next][a] = slot;
+    if (more) set_active(W, next, a, slot);
 }
 
 /* `sorted`: the list regrouped by shade key, else the active list as built
@@ -1182,7 +1202,7 @@ __global__ void k_wf_active_init(WfState W) {
     if (i >= W.slots) return;
     bool alive = (W.flags[i] & F_ALIVE) != 0;
     int a = warp_append(&W.ctr->n_active[0], alive);
-    if (alive) W.active[0][a] = i;
+    if (alive) set_active(W, 0, a, i);
 }
 
 /* Shade key of an active path: which code the shade kernel will run for it.
@@ -1249,7 +1269,8 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
         int first = 0;
         if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
         first = __shfl_sync(peers, first, leader);
-        W.sorted[base[key] + first + __popc(peers & ((1u << lane) - 1u))] = W.active[cur][i];
+        const int dst = base[key] + first + __popc(peers & ((1u << lane) - 1u));
+        if (in_bounds(W, dst, W.slots)) W.sorted[dst] = W.active[cur][i];
     }
 }
 

@@ -75,6 +75,7 @@ struct WfState {
     float4* q_o; float4* q_d; int32_t* q_meta;
     int32_t shadow_base;
     int32_t slots;
+    uint32_t* status;        /* the context's status word (RT_STATUS_*) */
     int32_t refill;          /* idle lanes of a trace warp before it fetches new rays */
     WfCounters* ctr;
     const WfJob* jobs;

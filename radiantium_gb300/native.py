@@ -20,6 +20,7 @@ RT_ERR_CANCELLED = -5
 RT_ERR_NO_SCENE = -6
 RT_ERR_UNSUPPORTED = -7
 RT_ERR_STACK = -8
+RT_ERR_BOUNDS = -9
 
 WRAP_CLAMP, WRAP_REPEAT = 0, 1
 FILTER_NEAREST, FILTER_LINEAR = 0, 1
@@ -144,7 +145,8 @@ def hit_dtype():
 
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
+# RADIANTIUM_GB300_LIB selects another build of the library (e.g. a debug-bounds variant)
+LIB_PATH = os.environ.get("RADIANTIUM_GB300_LIB") or os.path.join(PKG_DIR, "_lib", "libradiantium_gb300.so")
 
 # every symbol include/radiantium.h declares
 EXPORTED_SYMBOLS = [
