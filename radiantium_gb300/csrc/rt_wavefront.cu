@@ -1205,20 +1205,24 @@ __global__ void k_wf_active_init(WfState W) {
     if (alive) set_active(W, 0, a, i);
 }
 
-/* Shade key of an active path: which code the shade kernel will run for it.
+/* Code key of an active path: which code the shade kernel will run for it.
  * 0 finished (pending term, then a new sample), 1 missed the scene, 2 hit a
- * medium boundary without a surface, 3 + RT_MAT_* hit that material type. */
+ * medium boundary without a surface, 3 + RT_MAT_* hit that material type,
+ * 15 vol_path boundary walks.  The shade key puts the job (mod 16) above it,
+ * so a batch shades - and then traces - one scene's paths together. */
 DF int shade_key(const WfState& W, int slot) {
     const uint32_t fl = W.flags[slot];
-    if (fl & (F_WTR | F_WIT)) return WF_SHADE_KEYS - 1;     /* vol_path: advancing boundary walks */
-    if (fl & F_DONE) return 0;
+    const int job = W.job[slot];
+    const int jk = (job & 15) << 4;
+    if (fl & (F_WTR | F_WIT)) return jk | 15;
+    if (fl & F_DONE) return jk;
     const int hs = __float_as_int(W.ext_hit[slot].w);
-    if (hs < 0) return 1;
-    const RtSceneView* S = W.jobs[W.job[slot]].view;
+    if (hs < 0) return jk | 1;
+    const RtSceneView* S = W.jobs[job].view;
     const int prim = __float_as_int(__ldg(S->slots + 3 * (int64_t)hs).w);
     const int m = S->prims[prim].material;
-    if (m < 0) return 2;
-    return min(3 + S->materials[m].type, WF_SHADE_KEYS - 1);
+    if (m < 0) return jk | 2;
+    return jk | min(3 + S->materials[m].type, 14);
 }
 
 /* between trace and shade: the queues are consumed, reset their counters */
@@ -1228,7 +1232,7 @@ __global__ void k_wf_phase(WfState W) {
         c->n_closest = 0; c->n_shadow = 0; c->fetch[0] = 0; c->fetch[1] = 0; c->shade_fetch = 0;
         c->n_active[(c->iter & 1) ^ 1] = 0;
     }
-    if (threadIdx.x < 2 * WF_SHADE_KEYS) W.ctr->key_count[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < 2 * WF_SHADE_KEYS; k += blockDim.x) W.ctr->key_count[k] = 0;
 }
 
 /* both sort kernels are grid-stride loops: one pass with a grid sized to the
@@ -1247,17 +1251,25 @@ __global__ void __launch_bounds__(256) k_wf_sort_count(WfState W) {
 }
 
 /* counting-sort scatter: entries of one key stay together, in any order
- * (every path's result is independent of the order paths are shaded in) */
+ * (every path's result is independent of the order paths are shaded in).
+ * Each block turns the key counts into bases with a shared-memory scan. */
+static_assert(WF_SHADE_KEYS == 256, "the scatter's scan runs one thread per key in a 256-thread block");
 __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
     __shared__ int base[WF_SHADE_KEYS];
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     if ((int)(blockIdx.x * blockDim.x) >= n) return;
-    if (threadIdx.x < WF_SHADE_KEYS) {
-        int b = 0;
-        for (int k = 0; k < (int)threadIdx.x; k++) b += W.ctr->key_count[k];
-        base[threadIdx.x] = b;
+    const int t = threadIdx.x;
+    int v = W.ctr->key_count[t];
+    base[t] = v;
+    __syncthreads();
+    for (int off = 1; off < WF_SHADE_KEYS; off <<= 1) {      /* inclusive Hillis-Steele scan */
+        const int add = t >= off ? base[t - off] : 0;
+        __syncthreads();
+        base[t] += add;
+        __syncthreads();
     }
+    base[t] -= v;                                           /* exclusive */
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
     for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -1336,7 +1348,7 @@ cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned
     const WfAdjoint A = adj ? *adj : WfAdjoint{-1, 0, nullptr, nullptr, nullptr, nullptr};
     const bool known = n_hint >= 0;
     const int n = known ? std::min(n_hint, W.slots) : W.slots;
-    k_wf_phase<<<1, 2 * WF_SHADE_KEYS, 0, s>>>(W);
+    k_wf_phase<<<1, 256, 0, s>>>(W);
     if (n > 0) {
         const unsigned sb = known ? grid_for(n, 256) : (unsigned)sort_blocks;
         if (sort) {

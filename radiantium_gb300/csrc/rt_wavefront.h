@@ -25,7 +25,7 @@ enum { WF_RAY_SPLAT = 2 };
 
 #define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
 #define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
-#define WF_SHADE_KEYS 16
+#define WF_SHADE_KEYS 256          /* shade key: (job mod 16) * 16 + the path's code key (0..15) */
 #define WF_ITER_CAP (1 << 20)      /* bounce iterations of one round before a run gives up */
 
 /* one render of a batch, for the current round of samples (light tracing:
