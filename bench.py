@@ -621,7 +621,17 @@ def run_batch(args):
     alg_bytes_step = (B_RAY * (counts["rays_closest"] + counts["rays_shadow"]) + B_NODE * counts["node_visits"]
                       + B_PRIM * counts["prim_tests"] + B_INST * counts["instance_visits"] + B_FILM * counts["samples"])
     graph = mode == N.RENDERER_WAVEFRONT_GRAPH
-    achieved = alg_bytes_step / (loop_ms / args.steps / 1000.0) / 1e9
+    trace_ms, trace_shade_ms = loop_ms / args.steps, shade_ms / args.steps
+    if graph:
+        # the graph-driven loop is timed as a whole: the trace kernels' own time comes
+        # from one more (untimed) step of the host-driven loop over the same batch
+        host.set_renderer(N.RENDERER_WAVEFRONT)
+        host.render_batch_device(items(args.warmup), ptrs, stream)
+        torch.cuda.synchronize()
+        st = host.stats()
+        trace_ms, trace_shade_ms = st["render_kernel_ms"], st["shade_kernel_ms"]
+        host.set_renderer(mode)
+    achieved = alg_bytes_step / (trace_ms / 1000.0) / 1e9
     peak, peak_src = measured_peak()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -641,9 +651,10 @@ def run_batch(args):
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,
-                     "kernel": ("whole bounce loop (graph: trace + sort + shade)" if graph
-                                else "k_wf_trace_closest + k_wf_trace_shadow"),
-                     "kernel_ms_per_step": loop_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
+                     "kernel": "k_wf_trace_closest + k_wf_trace_shadow",
+                     "kernel_ms_per_step": trace_ms, "shade_ms_per_step": trace_shade_ms,
+                     "loop_ms_per_step": loop_ms / args.steps,
+                     "note": ("trace / shade times from one step of the host-driven loop" if graph else "")},
         "plain_megakernel": plain,
         "sequential_wavefront": seq_wf,
         "cpu_baseline": cpu,
