@@ -967,6 +967,23 @@ def run_particles(args):
                 raise RuntimeError(dev.lib.rt_last_error(dev.h).decode())
         e2e = {"value": per * world / float(np.mean(times)), "unit": "particles/s", "h2d_bytes_per_step": 0,
                "d2h_bytes_per_step": W * H * 12, "note": "rt_render_particles with a pinned host film"}
+    # the one-thread-per-particle megakernel on particle ranges of the same size
+    plain = None
+    if wavefront and args.plain_steps > 0:
+        dev.set_renderer(N.RENDERER_MEGAKERNEL)
+        pt = []
+        for i in range(args.plain_steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.render_particles_device(st, per, film.data_ptr(), first=base + (1 + args.warmup + i) * per,
+                                        stream=stream)
+            e1.record()
+            e1.synchronize()
+            pt.append(e0.elapsed_time(e1))
+        dev.set_renderer(mode)
+        plain = {"value": per / (float(np.mean(pt)) / 1000.0), "unit": "particles/s", "steps": args.plain_steps,
+                 "note": "megakernel k_particles (one thread per particle), same particle ranges"}
+
     # roofline of the traversal kernels: algorithmic bytes from exact counts (the
     # finishing pass's W*H camera rays are in the counts too; the splats' film
     # atomics are not).  The graph-driven loop is timed as a whole, so the trace
@@ -1008,6 +1025,7 @@ def run_particles(args):
                      "launches_per_step": rls, "shade_ms_per_step": sms,
                      "note": ("trace / shade times from one step of the host-driven loop"
                               if wavefront and mode != N.RENDERER_WAVEFRONT else "")},
+        "plain_megakernel": plain,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
                                                    "prim_tests", "instance_visits")},
