@@ -377,7 +377,7 @@ struct Best {
 
 #define RT_TRAVERSAL_CAP (1u << 26)   /* loop steps of one two-level traversal */
 #ifndef RT_DESCEND
-#define RT_DESCEND 2                   /* interior nodes one traversal step may visit */
+#define RT_DESCEND 2                   /* interior nodes one traversal step may visit (shallow trees) */
 #endif
 #define RT_NO_NODE ((int)0x80000000)
 
@@ -517,7 +517,7 @@ DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravS
 }
 
 /* One step; true when the traversal has finished. */
-template <class Stk>
+template <class Stk, int kDescend = RT_DESCEND>
 DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
     if (T.leafLeft > 0) {
@@ -573,8 +573,8 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        /* up to RT_DESCEND interior nodes (with the pops that follow them) per step */
-        for (int k = 0; k < RT_DESCEND && T.cur >= 0; k++) {
+        /* up to kDescend interior nodes (with the pops that follow them) per step */
+        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
             if (T.sp - T.base == RT_STACK_SIZE) {
                 atomicOr(status, RT_STATUS_STACK);
                 if (!T.inProto) return true;
@@ -665,7 +665,7 @@ DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st
 }
 
 /* One step; true when the traversal has finished (T.hit holds the answer). */
-template <class Stk>
+template <class Stk, int kDescend = RT_DESCEND>
 DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
     if (T.leafLeft > 0) {
@@ -704,7 +704,7 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, T
         return false;
     }
     if (T.cur != RT_NO_NODE) {
-        for (int k = 0; k < RT_DESCEND && T.cur >= 0; k++) {
+        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
             if (T.sp - T.base == RT_STACK_SIZE) {
                 atomicOr(status, RT_STATUS_STACK);
                 if (!T.inProto) return true;

@@ -230,6 +230,12 @@ DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
     else { W.trw_hit[path] = h; W.trw_sub[path] = T.best.sub; }
 }
 
+/* interior nodes per traversal step in scenes with tall trees (C2 / C3 trace: 94.5 / 25.5 ms
+ * at 2, 93.6 / 24.9 ms at 3; the shallow light-tracer scene is 1 % faster at 2) */
+#ifndef RT_DESCEND_DEEP
+#define RT_DESCEND_DEEP 3
+#endif
+
 /* The traversal stack of a trace kernel: with kSh (scenes with tall trees)
  * its bottom RT_SH_STACK entries live in shared memory, which keeps the stack
  * of a deep traversal out of the L1 lines the node data needs; shallow trees
@@ -274,7 +280,11 @@ __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_CLOSEST_BLOCKS) k_wf_trace_
                 else item = q;
             }
         }
-        if (item >= 0 && ClosestStep(S, T, stack, status, pst)) { closest_done(W, meta, T); done++; item = -1; }
+        if (item >= 0 && ClosestStep<decltype(stack), kSh ? RT_DESCEND_DEEP : RT_DESCEND>(S, T, stack, status, pst)) {
+            closest_done(W, meta, T);
+            done++;
+            item = -1;
+        }
     }
     if (counting) {
         warp_add64(stats + 1, done);
@@ -326,7 +336,7 @@ __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_SHADOW_BLOCKS) k_wf_trace_s
                 else item = q;
             }
         }
-        if (item >= 0 && AnyStep(S, T, stack, status, pst)) {
+        if (item >= 0 && AnyStep<decltype(stack), kSh ? RT_DESCEND_DEEP : RT_DESCEND>(S, T, stack, status, pst)) {
             shadow_done(W, meta, T.hit);
             done++;
             item = -1;
