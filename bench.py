@@ -170,14 +170,14 @@ def measured_peak():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def profiled_traffic(name):
-    """Per-sample DRAM traffic of the traversal kernels from the committed ncu
-    summary (profiles/trace_<workload>_traffic.txt: one line `bytes_per_sample=<x>`)."""
+def profiled_traffic(name, key="bytes_per_sample"):
+    """Per-sample (or per-particle) DRAM traffic of the traversal kernels from the
+    committed ncu summary (profiles/trace_<workload>_traffic.txt: one line `<key>=<x>`)."""
     p = os.path.join(ROOT, "profiles", f"trace_{name}_traffic.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("bytes_per_sample="):
+        if line.startswith(key + "="):
             return float(line.split("=", 1)[1])
     return None
 
@@ -1000,6 +1000,8 @@ def run_particles(args):
         dev.set_renderer(mode)
     achieved = alg / (kms / 1000.0) / 1e9
     peak, peak_src = measured_peak()
+    bpp = profiled_traffic("particle", "bytes_per_particle") if wavefront else None
+    traffic = None if bpp is None else bpp * per / max(1.0, rls)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
@@ -1019,7 +1021,7 @@ def run_particles(args):
                        + " + k_particle_finish"),
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_src,
+                     "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_wf_trace_closest + k_wf_trace_shadow" if wavefront else "k_particles",
                      "alg_bytes_per_step": alg, "kernel_ms_per_step": kms,
                      "launches_per_step": rls, "shade_ms_per_step": sms,
