@@ -315,8 +315,8 @@ def run_ours(args):
     value = samples_step * world / (ms_step / 1000.0)
 
     # relMSE of the frame the timed steps rendered, against an independent render
-    # at 8x its spp (SURVEY's converged-reference comparison; films of every
-    # renderer here are identical per sample, so equal spp means equal relMSE)
+    # at 8x its spp (a converged-reference comparison; films of every renderer
+    # here are identical per sample, so equal spp means equal relMSE)
     relmse = None
     if not args.no_relmse:
         frame_spp = spp_step * args.steps

@@ -1,7 +1,7 @@
 /*
  * oracle.h - C entry points of the CPU oracle (liboracle.so).
  *
- * TEST INFRASTRUCTURE ONLY: the checker the CUDA library is compared with.
+ * TEST INFRASTRUCTURE ONLY: the reference restatement the CUDA library is compared with.
  * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load it.
  * It consumes the same rt_scene_desc as the library (include/radiantium.h).
  */
