@@ -804,6 +804,77 @@ RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64
 
 void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true, bool deep = false);
 
+/* What a wavefront run shades, and how its kernels are chosen. */
+struct WfMode {
+    bool vol = false;        /* vol_path shade kernel */
+    bool particle = false;   /* light-tracer start / shade kernels */
+    bool sort = true;        /* regroup the active list by shade key before shading */
+    bool deep = false;       /* trace kernels with the shared-memory stack (trees of 16+ levels) */
+};
+/* CUDA-event times and launch counts of a run, summed over its rounds */
+struct WfTotals {
+    double trace_ms = 0, shade_ms = 0;
+    uint64_t launches = 0, trace_launches = 0;
+};
+
+/* One round of a wavefront run over the jobs already in c->d_jobs: every slot
+ * takes a sample (or particle), then the loop bounces until no path is active
+ * and no splat ray is queued (a finished particle leaves its last one behind).
+ * The loop runs as one CUDA graph launch (render passes with `use_graph`) or
+ * is driven from the host with per-phase event timing. */
+void wf_round(Ctx* c, const WfState& W, cudaStream_t s, bool use_graph, const WfMode& m, int pass,
+              const WfAdjoint* adj, int64_t total, int n_jobs, WfTotals* t) {
+    std::memset(c->h_ctr, 0, sizeof(WfCounters));
+    c->h_ctr->total = total;
+    c->h_ctr->n_jobs = n_jobs;
+    CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+    CK(rt_wf_start(W, s, m.particle));
+    t->launches += 2;
+    if (use_graph && pass == WF_PASS_RENDER) {
+        ensure_wf_graph(c, W, m.vol, m.particle, m.sort, m.deep);
+        CK(cudaEventRecord(c->events[0], s));
+        CK(cudaGraphLaunch(c->wf_exec, s));
+        CK(cudaEventRecord(c->events[1], s));
+        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
+        t->launches += (m.sort ? 7 : 5) * iters;
+        t->trace_launches += 2 * iters;
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, c->events[0], c->events[1]));
+        t->trace_ms += ms;                     /* the whole loop: not split by phase */
+        return;
+    }
+    CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
+        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+        NvtxRange nvtx_iter("rt.wavefront_iteration");
+        CK(cudaEventRecord(c->events[0], s));
+        CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, m.deep));
+        CK(cudaEventRecord(c->events[1], s));
+        CK(cudaEventRecord(c->events[2], s));
+        CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false, s,
+                       &t->launches, pass, adj, m.vol, m.particle, m.sort));
+        CK(cudaEventRecord(c->events[3], s));
+        t->launches += 2;
+        t->trace_launches += 2;
+        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, c->events[0], c->events[1])); t->trace_ms += ms;
+        CK(cudaEventElapsedTime(&ms, c->events[2], c->events[3])); t->shade_ms += ms;
+    }
+}
+
+void wf_store_totals(Ctx* c, const WfTotals& t) {
+    c->last.render_kernel_ms = t.trace_ms;
+    c->last.shade_kernel_ms = t.shade_ms;
+    c->last.render_launches = t.trace_launches;
+    c->last.kernel_launches = t.launches;
+}
+
 /* The light tracer as a wavefront (rt_wavefront.cu): rounds of up to
  * 4 x sample_budget particles (cancellation is checked between rounds); in
  * a round, path slots are refilled with the next particle until none is
@@ -820,9 +891,11 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
     W.slots = slots;
     W.shadow_base = 2 * slots;
     W.refill = c->wf_refill;
-    const bool sort = c->mat_types > 1, deep = c->tallest >= RT_DEEP_TREE;
-    uint64_t launches = 0, trace_launches = 0;
-    double trace_ms = 0, shade_ms = 0;
+    WfMode m;
+    m.particle = true;
+    m.sort = c->mat_types > 1;
+    m.deep = c->tallest >= RT_DEEP_TREE;
+    WfTotals t;
     for (int64_t done = 0; done < count;) {
         if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
         const int64_t n = std::min(round_max, count - done);
@@ -834,55 +907,10 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
         d.first = first + done;
         d.count = n;
         CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(WfJob), cudaMemcpyHostToDevice, s));
-        std::memset(c->h_ctr, 0, sizeof(WfCounters));
-        c->h_ctr->total = n;
-        c->h_ctr->n_jobs = 1;
-        CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
-        CK(rt_wf_start(W, s, true));
-        launches += 2;
-        if (use_graph) {
-            ensure_wf_graph(c, W, false, true, sort, deep);
-            CK(cudaEventRecord(c->events[0], s));
-            CK(cudaGraphLaunch(c->wf_exec, s));
-            CK(cudaEventRecord(c->events[1], s));
-            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
-            launches += (sort ? 7 : 5) * iters;
-            trace_launches += 2 * iters;
-            float t = 0;
-            CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
-            trace_ms += t;                     /* the whole loop: not split by phase */
-        } else {
-            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            /* a finished particle's last splat ray is still queued when its slot leaves the active list */
-            while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
-                if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-                if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
-                NvtxRange nvtx_iter("rt.wavefront_iteration");
-                CK(cudaEventRecord(c->events[0], s));
-                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
-                CK(cudaEventRecord(c->events[1], s));
-                CK(cudaEventRecord(c->events[2], s));
-                CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
-                               s, &launches, WF_PASS_RENDER, nullptr, false, true, sort));
-                CK(cudaEventRecord(c->events[3], s));
-                launches += 2;
-                trace_launches += 2;
-                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                float t = 0;
-                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
-                CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
-            }
-        }
+        wf_round(c, W, s, use_graph, m, WF_PASS_RENDER, nullptr, n, 1, &t);
         done += n;
     }
-    c->last.render_kernel_ms = trace_ms;
-    c->last.shade_kernel_ms = shade_ms;
-    c->last.render_launches = trace_launches;
-    c->last.kernel_launches = launches;
+    wf_store_totals(c, t);
 }
 
 /* AdjointParticleRenderer (Renderers/AdjointParticleRenderer.cs:118-172): the
@@ -1098,12 +1126,12 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
      * from it when rendering.  vol_path keys also separate medium-boundary hits and paths advancing
      * boundary walks, and the adjoint replay's gradient scatter gains from grouped paths (C5: 22.1
      * gradients/s unsorted, 28.5 sorted), so both keep it. */
-    const bool sort = vol || adj || jobs.size() > 1 || jobs[0].mat_types > 1;
-    bool deep = false;
-    for (const WfJobIn& J : jobs) deep = deep || J.tallest >= RT_DEEP_TREE;
+    WfMode mode;
+    mode.vol = vol;
+    mode.sort = vol || adj || jobs.size() > 1 || jobs[0].mat_types > 1;
+    for (const WfJobIn& J : jobs) mode.deep = mode.deep || J.tallest >= RT_DEEP_TREE;
     ensure_events(c, 4);
-    double trace_ms = 0, shade_ms = 0;
-    uint64_t launches = 0, trace_launches = 0;
+    WfTotals tot;
     while (true) {
         if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
         std::vector<int> act;
@@ -1143,48 +1171,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         W.refill = c->wf_refill;
         /* one pass over the round's samples: start every slot, bounce until no path is left */
         auto run_pass = [&](int pass) {
-            std::memset(c->h_ctr, 0, sizeof(WfCounters));
-            c->h_ctr->total = total;
-            c->h_ctr->n_jobs = (int)act.size();
-            CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
-            CK(rt_wf_start(W, s));
-            launches += 2;
-            if (use_graph && pass == WF_PASS_RENDER) {
-                ensure_wf_graph(c, W, vol, false, sort, deep);
-                CK(cudaEventRecord(c->events[0], s));
-                CK(cudaGraphLaunch(c->wf_exec, s));
-                CK(cudaEventRecord(c->events[1], s));
-                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                const uint64_t iters = (uint64_t)std::max(0, c->h_ctr->iter);
-                launches += (sort ? 7 : 5) * iters;
-                trace_launches += 2 * iters;
-                float t = 0;
-                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1]));
-                trace_ms += t;                  /* the whole loop: not split by phase */
-                return;
-            }
-            CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0) {
-                if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-                if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
-                NvtxRange nvtx_iter("rt.wavefront_iteration");
-                CK(cudaEventRecord(c->events[0], s));
-                CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, deep));
-                CK(cudaEventRecord(c->events[1], s));
-                CK(cudaEventRecord(c->events[2], s));
-                CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false,
-                               s, &launches, pass, adj, vol, false, sort));
-                CK(cudaEventRecord(c->events[3], s));
-                launches += 2;
-                trace_launches += 2;
-                CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(WfCounters), cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                float t = 0;
-                CK(cudaEventElapsedTime(&t, c->events[0], c->events[1])); trace_ms += t;
-                CK(cudaEventElapsedTime(&t, c->events[2], c->events[3])); shade_ms += t;
-            }
+            wf_round(c, W, s, use_graph, mode, pass, adj, total, (int)act.size(), &tot);
         };
         if (adj) {
             run_pass(WF_PASS_FORWARD_RAW);
@@ -1196,14 +1183,11 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         for (size_t k = 0; k < act.size(); k++) {
             const WfJobIn& J = jobs[act[k]];
             CK(rt_launch_accumulate(J.film, c->h_jobs[k].samples, (int64_t)J.P.w * J.P.h, clen[k], s));
-            launches += 1;
+            tot.launches += 1;
             done[act[k]] += clen[k];
         }
     }
-    c->last.render_kernel_ms = trace_ms;
-    c->last.shade_kernel_ms = shade_ms;
-    c->last.render_launches = trace_launches;
-    c->last.kernel_launches = launches;
+    wf_store_totals(c, tot);
 }
 
 void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t s) {
