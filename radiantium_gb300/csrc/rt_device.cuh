@@ -484,9 +484,11 @@ DF void EnterLeaf(const RtSceneView* S, int* cur, int* leafSlot, int* leafLeft) 
  * leaf, InstancedPrimitive.Intersect (Primitive.cs:169-188) on its prototype
  * tree in model space with world T = Distance(ray.O, p).  Boxes, MaxT culls
  * and primitive tests happen in exactly the order of the recursive form; the
- * recursion is unrolled into a state machine whose every step is one leaf
- * primitive, one node, one pop, or leaving a prototype.  Rays at different
- * levels therefore run the same step code together, and a persistent kernel
+ * recursion is unrolled into a state machine: a step visits up to kDescend
+ * interior nodes (with the pops that follow them) and then, if that reached a
+ * leaf, tests its next primitive, or leaves a prototype.  A lane that has just
+ * reached a leaf tests it together with the lanes already in leaves, and rays
+ * at different levels run the same step code together; a persistent kernel
  * can hand a lane a new ray between any two steps.  stack[0, base) holds
  * top-level entries, stack[base, base + RT_STACK_SIZE) the prototype's, so
  * `stack` has 2 * RT_STACK_SIZE entries. */
@@ -520,6 +522,23 @@ DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravS
 template <class Stk, int kDescend = RT_DESCEND>
 DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (T.cur != RT_NO_NODE) {
+        /* up to kDescend interior nodes (with the pops that follow them) per step */
+        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
+            if (T.sp - T.base == RT_STACK_SIZE) {
+                atomicOr(status, RT_STATUS_STACK);
+                if (!T.inProto) return true;
+                T.sp = T.base;                  /* the prototype's traversal stops here */
+                T.cur = RT_NO_NODE;
+                return false;
+            }
+            if (st) st->nodes++;
+            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+        }
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+        if (T.cur != RT_NO_NODE) return false;      /* still descending: the next step goes on */
+    }
     if (T.leafLeft > 0) {
         const int slot = T.leafSlot++;
         T.leafLeft--;
@@ -569,23 +588,6 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
         T.inProto = true;
         T.base = T.sp;
         T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
-        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
-        return false;
-    }
-    if (T.cur != RT_NO_NODE) {
-        /* up to kDescend interior nodes (with the pops that follow them) per step */
-        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
-            if (T.sp - T.base == RT_STACK_SIZE) {
-                atomicOr(status, RT_STATUS_STACK);
-                if (!T.inProto) return true;
-                T.sp = T.base;                  /* the prototype's traversal stops here */
-                T.cur = RT_NO_NODE;
-                return false;
-            }
-            if (st) st->nodes++;
-            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
-            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
-        }
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
@@ -668,6 +670,22 @@ DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st
 template <class Stk, int kDescend = RT_DESCEND>
 DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, TravStats* st) {
     if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (T.cur != RT_NO_NODE) {
+        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
+            if (T.sp - T.base == RT_STACK_SIZE) {
+                atomicOr(status, RT_STATUS_STACK);
+                if (!T.inProto) return true;
+                T.sp = T.base;
+                T.cur = RT_NO_NODE;
+                return false;
+            }
+            if (st) st->nodes++;
+            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
+        }
+        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
+        if (T.cur != RT_NO_NODE) return false;
+    }
     if (T.leafLeft > 0) {
         const int slot = T.leafSlot++;
         T.leafLeft--;
@@ -700,22 +718,6 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, T
         T.inProto = true;
         T.base = T.sp;
         T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
-        EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
-        return false;
-    }
-    if (T.cur != RT_NO_NODE) {
-        for (int k = 0; k < kDescend && T.cur >= 0; k++) {
-            if (T.sp - T.base == RT_STACK_SIZE) {
-                atomicOr(status, RT_STATUS_STACK);
-                if (!T.inProto) return true;
-                T.sp = T.base;
-                T.cur = RT_NO_NODE;
-                return false;
-            }
-            if (st) st->nodes++;
-            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
-            if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
-        }
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
