@@ -377,7 +377,9 @@ struct Best {
 
 #define RT_TRAVERSAL_CAP (1u << 26)   /* loop steps of one two-level traversal */
 #ifndef RT_DESCEND
-#define RT_DESCEND 2                   /* interior nodes one traversal step may visit (shallow trees) */
+/* interior nodes one traversal step may visit in shallow trees (Cornell box / light tracer,
+ * M samples / particles per s: 415 / 223 at 2, 421 / 229 at 3, 426 / 227 at 4, 418 / 224 at 5) */
+#define RT_DESCEND 3
 #endif
 #define RT_NO_NODE ((int)0x80000000)
 

@@ -230,10 +230,10 @@ DF void closest_done(const WfState& W, int meta, const TravClosest& T) {
     else { W.trw_hit[path] = h; W.trw_sub[path] = T.best.sub; }
 }
 
-/* interior nodes per traversal step in scenes with tall trees (C2 / C3 trace: 94.5 / 25.5 ms
- * at 2, 93.6 / 24.9 ms at 3; the shallow light-tracer scene is 1 % faster at 2) */
+/* interior nodes per traversal step in scenes with tall trees (C2 / C3 trace ms per step:
+ * 85.7 / 24.3 at 3, 83.7 / 23.8 at 4, 83.5 / 23.7 at 5, 87.5 / 23.2 at 6) */
 #ifndef RT_DESCEND_DEEP
-#define RT_DESCEND_DEEP 3
+#define RT_DESCEND_DEEP 5
 #endif
 
 /* The traversal stack of a trace kernel: with kSh (scenes with tall trees)
