@@ -63,6 +63,10 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+#ifndef RT_WF_REFILL
+#define RT_WF_REFILL 8                     /* default refill threshold of the trace warps */
+#endif
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -105,7 +109,7 @@ struct Ctx {
     WfJob* d_jobs = nullptr;                   /* device job table (WF_MAX_JOBS entries) */
     WfJob* h_jobs = nullptr;                   /* pinned staging of the job table */
     int wf_capacity = WF_MAX_SLOTS;            /* path slots in flight */
-    int wf_refill = 8;                         /* idle lanes before a trace warp fetches (1..32) */
+    int wf_refill = RT_WF_REFILL;              /* idle lanes before a trace warp fetches (1..32) */
     bool wf_graph_pref = false;                /* RT_RENDERER_AUTO drives the wavefront as a graph */
     int gpu_build_min = 1 << 15;               /* trees of at least this many primitives build on the GPU */
     uint64_t wf_generation = 0;                /* bumped whenever the path-state buffers move */
