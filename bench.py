@@ -335,7 +335,7 @@ def run_ours(args):
         import ctypes as C
         p = host.ctypes.data_as(C.c_void_p)
         lib, h = dev.lib, dev.h
-        times = []
+        times, h2d = [], []
         for i in range(args.steps):
             prm = st.replace(spp=spp_step, sample_begin=base + (args.warmup + args.steps + i) * spp_step).to_c()
             t0 = time.perf_counter()
@@ -343,11 +343,13 @@ def run_ours(args):
             times.append(time.perf_counter() - t0)
             if rc != 0:
                 raise RuntimeError(lib.rt_last_error(h).decode())
+            h2d.append(dev.stats()["h2d_bytes"])     # job tables and queue counters the call copied
         e2e_s = float(np.mean(times))
-        e2e = {"value": samples_step * world / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": 0,
+        e2e = {"value": samples_step * world / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": int(np.mean(h2d)),
                "d2h_bytes_per_step": npix * 12,
                "note": "rt_render with a pinned host film; scene resident (rt_upload_scene once, "
-                       f"{upload_s:.2f} s incl. BVH builds)"}
+                       f"{upload_s:.2f} s incl. BVH builds); h2d = the job tables and queue counters the "
+                       "call copies (rt_stats.h2d_bytes)"}
 
     # the plain megakernel on the same passes, for the wavefront / megakernel ratio
     plain = None
@@ -584,12 +586,14 @@ def run_batch(args):
 
     e2e = None
     if not args.no_e2e:
-        times = []
+        times, h2d = [], []
         for i in range(args.steps):
             t0 = time.perf_counter()
             host.render_batch(items(args.warmup + args.steps + i))
             times.append(time.perf_counter() - t0)
-        e2e = {"value": samples_step * world / float(np.mean(times)), "unit": "samples/s", "h2d_bytes_per_step": 0,
+            h2d.append(host.stats()["h2d_bytes"])
+        e2e = {"value": samples_step * world / float(np.mean(times)), "unit": "samples/s",
+               "h2d_bytes_per_step": int(np.mean(h2d)),
                "d2h_bytes_per_step": int(sum(s.camera.width * s.camera.height * 12 for s, _ in scenes)),
                "note": f"rt_render_batch into host films; scenes resident (32 x rt_upload_scene, {upload_s:.1f} s "
                        "incl. BVH builds)"}
@@ -724,11 +728,13 @@ def run_adjoint(args):
 
     for i in range(args.warmup):
         step(i)
+    d.render(st.replace(seed=base))
+    fwd_h2d = d.stats()["h2d_bytes"]                 # what a forward render copies from the host (untimed)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     if dist:
         dist.barrier()
-    times, bwd_ms, fwd_times = [], 0.0, []
+    times, bwd_ms, fwd_times, bwd_h2d = [], 0.0, [], []
     for i in range(args.steps):
         t0 = time.perf_counter()
         stx = st.replace(seed=base + args.warmup + i)
@@ -739,6 +745,7 @@ def run_adjoint(args):
         times.append(time.perf_counter() - t0)
         fwd_times.append(t1 - t0)
         bwd_ms += d.stats()["render_kernel_ms"]
+        bwd_h2d.append(d.stats()["h2d_bytes"])
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -803,7 +810,8 @@ def run_adjoint(args):
                     "vs_fd": (n_params / s_step) / (1.0 / (2.0 * fwd_s)),
                     "fd_check": check},
         "cpu_baseline": cpu,
-        "e2e": {"value": samples_step * world / s_step, "unit": "samples/s", "h2d_bytes_per_step": W * H * 12,
+        "e2e": {"value": samples_step * world / s_step, "unit": "samples/s",
+                "h2d_bytes_per_step": int(fwd_h2d + np.mean(bwd_h2d)),
                 "d2h_bytes_per_step": W * H * 12 + int(n_params) * 4,
                 "note": "the step is timed end to end through the C ABI: film to host, dL/dI from host, gradients to host"},
         "gpu_launches": None,
@@ -957,7 +965,7 @@ def run_particles(args):
         host = torch.empty(W * H * 3, dtype=torch.float32, pin_memory=True).numpy()
         p = host.ctypes.data_as(C.c_void_p)
         prm = st.to_c()
-        times = []
+        times, h2d = [], []
         for i in range(args.steps):
             t0 = time.perf_counter()
             rc = dev.lib.rt_render_particles(dev.h, C.byref(prm), base + (1 + args.warmup + args.steps + i) * per,
@@ -965,7 +973,9 @@ def run_particles(args):
             times.append(time.perf_counter() - t0)
             if rc != 0:
                 raise RuntimeError(dev.lib.rt_last_error(dev.h).decode())
-        e2e = {"value": per * world / float(np.mean(times)), "unit": "particles/s", "h2d_bytes_per_step": 0,
+            h2d.append(dev.stats()["h2d_bytes"])
+        e2e = {"value": per * world / float(np.mean(times)), "unit": "particles/s",
+               "h2d_bytes_per_step": int(np.mean(h2d)),
                "d2h_bytes_per_step": W * H * 12, "note": "rt_render_particles with a pinned host film"}
     # the one-thread-per-particle megakernel on particle ranges of the same size
     plain = None

@@ -236,7 +236,8 @@ typedef struct rt_stats {
     double render_kernel_ms;  /* summed duration of the path-tracing launches (CUDA events on their stream):
                                  the megakernel, or the wavefront traversal kernel */
     double shade_kernel_ms;   /* wavefront shading kernel (0 for the megakernel) */
-    uint64_t reserved[1];
+    uint64_t h2d_bytes;       /* bytes the call copied from host memory to the device: wavefront job
+                                 tables and queue counters, rays, dL/dI (kernel arguments not counted) */
 } rt_stats;
 
 /* ---- entry points ------------------------------------------------------ */

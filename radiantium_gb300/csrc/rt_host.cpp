@@ -96,6 +96,7 @@ struct Ctx {
     void* io = nullptr; size_t io_bytes = 0;   /* device staging for host-pointer calls */
     bool counting = false;
     rt_stats last{};
+    uint64_t h2d = 0;                          /* host -> device bytes copied by the current call */
     std::atomic<int> cancel{0};
     int64_t sample_budget = 1 << 24;          /* samples per launch (sample buffer = 12 B each) */
     std::vector<cudaEvent_t> events;           /* per-launch timing of the path-tracing kernel */
@@ -118,6 +119,12 @@ struct Ctx {
     cudaGraphExec_t wf_exec = nullptr;
     uint64_t wf_graph_key = 0;                 /* generation, slots and counting it was built for */
 };
+
+/* Host -> device copy on `s`, counted in the call's rt_stats.h2d_bytes. */
+void h2d(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    c->h2d += bytes;
+}
 
 void ensure_events(Ctx* c, size_t n) {
     while (c->events.size() < n) {
@@ -754,6 +761,7 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     double rms = c->last.render_kernel_ms, sms = c->last.shade_kernel_ms;
     uint64_t launches = c->last.kernel_launches, rl = c->last.render_launches;
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     read_stats(c);
     c->last.samples = (uint64_t)npix * P.spp;
     c->last.render_kernel_ms = rms;
@@ -831,7 +839,7 @@ void wf_round(Ctx* c, const WfState& W, cudaStream_t s, bool use_graph, const Wf
     std::memset(c->h_ctr, 0, sizeof(WfCounters));
     c->h_ctr->total = total;
     c->h_ctr->n_jobs = n_jobs;
-    CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(WfCounters), cudaMemcpyHostToDevice, s));
+    h2d(c, c->d_ctr, c->h_ctr, sizeof(WfCounters), s);
     CK(rt_wf_start(W, s, m.particle));
     t->launches += 2;
     if (use_graph && pass == WF_PASS_RENDER) {
@@ -910,7 +918,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
         d.samples = film;
         d.first = first + done;
         d.count = n;
-        CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(WfJob), cudaMemcpyHostToDevice, s));
+        h2d(c, c->d_jobs, c->h_jobs, sizeof(WfJob), s);
         wf_round(c, W, s, use_graph, m, WF_PASS_RENDER, nullptr, n, 1, &t);
         done += n;
     }
@@ -968,6 +976,7 @@ void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t 
         ms += t;
     }
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     read_stats(c);
     c->last.samples = (uint64_t)count;
     if (mega) {
@@ -1058,6 +1067,7 @@ void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t 
     CK(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     c->last.samples = (uint64_t)npix * P.spp;
     c->last.render_launches = chunks;
     c->last.kernel_launches = launches + 1;
@@ -1168,7 +1178,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
             d.count = (int64_t)J.P.w * J.P.h * clen[k];
             first += d.count;
         }
-        CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, act.size() * sizeof(WfJob), cudaMemcpyHostToDevice, s));
+        h2d(c, c->d_jobs, c->h_jobs, act.size() * sizeof(WfJob), s);
         WfState W = c->wf;
         W.slots = slots;
         W.shadow_base = 2 * slots;
@@ -1270,6 +1280,7 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
     double rms = c->last.render_kernel_ms, sms = c->last.shade_kernel_ms;
     uint64_t launches = c->last.kernel_launches, rl = c->last.render_launches;
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     read_stats(c);
     c->last.samples = samples;
     c->last.render_kernel_ms = rms;
@@ -1319,8 +1330,8 @@ void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* 
     ensure(&c->adj_galb, &c->adj_galb_bytes, (size_t)std::max<int64_t>(1, texels) * 12);
     ensure(&c->adj_galpha, &c->adj_galpha_bytes, (size_t)std::max(1, d->alpha_count) * 4);
     ensure(&c->adj_slot, &c->adj_slot_bytes, slot.size() * 4);
-    CK(cudaMemcpyAsync(c->adj_dldi, dldi, (size_t)npix * 12, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(c->adj_slot, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice, s));
+    h2d(c, c->adj_dldi, dldi, (size_t)npix * 12, s);
+    h2d(c, c->adj_slot, slot.data(), slot.size() * 4, s);
     CK(rt_launch_scale(c->adj_dldi, npix * 3, 1.0f / (float)P.spp, s));
     CK(cudaMemsetAsync(c->adj_galb, 0, (size_t)std::max<int64_t>(1, texels) * 12, s));
     CK(cudaMemsetAsync(c->adj_galpha, 0, (size_t)std::max(1, d->alpha_count) * 4, s));
@@ -1365,6 +1376,7 @@ void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     c->last.samples = (uint64_t)npix * P.spp;
     c->last.render_kernel_ms = ms;
     c->last.kernel_launches = launches;
@@ -1434,7 +1446,7 @@ void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bo
         size_t out_bytes = hits ? (size_t)n * sizeof(rt_hit) : (size_t)n;
         ensure(&c->io, &c->io_bytes, (size_t)n * sizeof(rt_ray) + out_bytes + 256);
         char* base = (char*)c->io;
-        CK(cudaMemcpyAsync(base, rays, (size_t)n * sizeof(rt_ray), cudaMemcpyHostToDevice, s));
+        h2d(c, base, rays, (size_t)n * sizeof(rt_ray), s);
         dr = (const rt_ray*)base;
         char* ob = base + (((size_t)n * sizeof(rt_ray) + 255) & ~(size_t)255);
         if (hits) dh = (rt_hit*)ob; else dob = (uint8_t*)ob;
@@ -1447,6 +1459,7 @@ void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bo
     CK(cudaStreamSynchronize(s));
     check_status(c);
     std::memset(&c->last, 0, sizeof(c->last));
+    c->last.h2d_bytes = c->h2d;
     read_stats(c);
     if (hits) c->last.rays_closest = (uint64_t)n; else c->last.rays_shadow = (uint64_t)n;
     c->last.kernel_launches = n > 0 ? 1 : 0;
@@ -1457,6 +1470,7 @@ int run(Ctx* c, F f) {
     if (!c) return RT_ERR_INVALID_ARG;
     try {
         CK(cudaSetDevice(c->device));
+        c->h2d = 0;
         f();
         c->err.clear();
         return RT_OK;

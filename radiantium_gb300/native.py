@@ -124,10 +124,10 @@ class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64),
                 ("node_visits", C.c_uint64), ("prim_tests", C.c_uint64), ("instance_visits", C.c_uint64),
                 ("invalid_samples", C.c_uint64), ("kernel_launches", C.c_uint64), ("render_launches", C.c_uint64),
-                ("render_kernel_ms", C.c_double), ("shade_kernel_ms", C.c_double), ("reserved", C.c_uint64 * 1)]
+                ("render_kernel_ms", C.c_double), ("shade_kernel_ms", C.c_double), ("h2d_bytes", C.c_uint64)]
 
     def as_dict(self):
-        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k not in ("reserved", "render_kernel_ms", "shade_kernel_ms")}
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k not in ("render_kernel_ms", "shade_kernel_ms")}
         d["render_kernel_ms"] = float(self.render_kernel_ms)
         d["shade_kernel_ms"] = float(self.shade_kernel_ms)
         return d

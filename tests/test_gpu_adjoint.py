@@ -64,6 +64,14 @@ def test_forward_is_the_render(adj):
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
+def test_backward_counts_its_host_copies(adj):
+    """rt_stats.h2d_bytes of the backward pass: dL/dI (w * h * 3 floats) plus its small tables."""
+    d, st, prm, _, _, w, _ = adj
+    d.adjoint_backward(st.replace(spp=2, seed=4), w, prm["albedo_texture"], prm["alpha_materials"])
+    h = d.stats()["h2d_bytes"]
+    assert w.size * 4 < h < w.size * 4 + (1 << 16)
+
+
 def test_albedo_gradient_matches_fd(adj):
     d, st, prm, alb0, alpha0, w, set_params = adj
     stx = st.replace(spp=256, seed=3)

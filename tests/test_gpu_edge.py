@@ -120,3 +120,31 @@ def test_depth_limit_before_the_first_bounce(dev, max_depth):
             assert np.array_equal(_bits(dev.render_particles(pst, 3000)), _bits(pwant)), mode
     finally:
         dev.set_renderer(N.RENDERER_AUTO)
+
+
+def test_h2d_byte_counts(dev):
+    """rt_stats.h2d_bytes counts what a call copies from host memory to the device: a host ray
+    batch exactly its rays, the megakernel nothing (its parameters are kernel arguments), a
+    wavefront render its job table and queue counters (a few hundred bytes per round)."""
+    s, st = procedural.cornell_box(32, 24)
+    dev.upload(s)
+    rays = np.zeros(100, dtype=N.ray_dtype())
+    rays["o"][:] = (0.0, 0.5, 0.0)
+    rays["d"][:] = (0.0, 0.0, 1.0)
+    rays["min_t"], rays["max_t"] = 1e-4, 1e30
+    dev.trace_closest(rays)
+    assert dev.stats()["h2d_bytes"] == rays.nbytes
+    dev.trace_any(rays)
+    assert dev.stats()["h2d_bytes"] == rays.nbytes
+    try:
+        dev.set_renderer(N.RENDERER_MEGAKERNEL)
+        dev.render(st.replace(spp=2))
+        assert dev.stats()["h2d_bytes"] == 0
+        for m in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH):
+            dev.set_renderer(m)
+            dev.render(st.replace(spp=2))
+            assert 0 < dev.stats()["h2d_bytes"] < 1 << 16, m
+            dev.render_particles(st.replace(integrator=N.INTEGRATOR_PARTICLE), 5000)
+            assert 0 < dev.stats()["h2d_bytes"] < 1 << 16, m
+    finally:
+        dev.set_renderer(N.RENDERER_AUTO)
