@@ -729,12 +729,13 @@ def run_adjoint(args):
     for i in range(args.warmup):
         step(i)
     d.render(st.replace(seed=base))
-    fwd_h2d = d.stats()["h2d_bytes"]                 # what a forward render copies from the host (untimed)
+    fwd = d.stats()                                  # what a forward render copies and launches (untimed)
+    fwd_h2d, fwd_launches = fwd["h2d_bytes"], fwd["kernel_launches"]
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     if dist:
         dist.barrier()
-    times, bwd_ms, fwd_times, bwd_h2d = [], 0.0, [], []
+    times, bwd_ms, fwd_times, bwd_h2d, bwd_launches = [], 0.0, [], [], 0
     for i in range(args.steps):
         t0 = time.perf_counter()
         stx = st.replace(seed=base + args.warmup + i)
@@ -746,6 +747,7 @@ def run_adjoint(args):
         fwd_times.append(t1 - t0)
         bwd_ms += d.stats()["render_kernel_ms"]
         bwd_h2d.append(d.stats()["h2d_bytes"])
+        bwd_launches += d.stats()["kernel_launches"]
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -814,7 +816,7 @@ def run_adjoint(args):
                 "h2d_bytes_per_step": int(fwd_h2d + np.mean(bwd_h2d)),
                 "d2h_bytes_per_step": W * H * 12 + int(n_params) * 4,
                 "note": "the step is timed end to end through the C ABI: film to host, dL/dI from host, gradients to host"},
-        "gpu_launches": None,
+        "gpu_launches": int(fwd_launches * args.steps + bwd_launches),
         "clocks": clk,
     }
     if rank == 0:
