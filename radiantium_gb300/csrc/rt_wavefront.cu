@@ -72,6 +72,26 @@ DF int warp_append(int* counter, bool want) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+/* Block-aggregated append: one atomic per block.  Every thread of the block
+ * calls it (blockDim.x a multiple of 32, at most 1024). */
+DF int block_append(int* counter, bool want) {
+    __shared__ int s_cnt[32];
+    __shared__ int s_base;
+    const unsigned b = __ballot_sync(0xffffffffu, want);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) s_cnt[w] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < nw; k++) { const int c = s_cnt[k]; s_cnt[k] = t; t += c; }
+        s_base = t ? atomicAdd(counter, t) : 0;
+    }
+    __syncthreads();
+    const int r = want ? s_base + s_cnt[w] + __popc(b & ((1u << lane) - 1u)) : -1;
+    __syncthreads();
+    return r;
+}
+
 /* Debug-bounds builds (-DRT_DEBUG_BOUNDS) check every computed index into a
  * path-state buffer: one outside its buffer sets RT_STATUS_BOUNDS and the
  * access is skipped (no trap), so the host reports RT_ERR_BOUNDS. */
@@ -401,7 +421,7 @@ DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned
 /* one bounce of PathTracer.Mis / NextEventEstimation / OnlySampleBxdf after the
  * extension hit is known (PathTracer.cs:43-270) */
 template <bool kAdj>
-DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting,
+DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting,
                    int pass, const WfAdjoint& A, float* s_alpha) {
     const WfJob& J = W.jobs[W.job[slot]];
     const RtSceneView* S = J.view;
@@ -639,19 +659,13 @@ DF void shade_path(const WfState& W, int slot, int next, uint32_t* status, unsig
     /* the slot stays active while it waits for rays */
     if ((fl & F_PENDING) || !(fl & F_DONE)) {
         W.flags[slot] = fl;
-        int a = warp_append(&W.ctr->n_active[next], true);
-        set_active(W, next, a, slot);
-        return;
+        return true;
     }
     finish_path(J, W, slot, radiance, stats, pass);
     if (counting) warp_add64(stats + 0, 1u);
-    if (start_path(W, slot, true)) {
-        int a = warp_append(&W.ctr->n_active[next], true);
-        set_active(W, next, a, slot);
-    } else {
-        W.flags[slot] = 0;
-        warp_append(&W.ctr->n_active[next], false);
-    }
+    if (start_path(W, slot, true)) return true;
+    W.flags[slot] = 0;
+    return false;
 }
 
 /* ---- vol_path (VolumetricPathTracer.Li, Integrators/VolumetricPathTracer.cs) ----
@@ -755,7 +769,7 @@ DF bool itw_step(const RtSceneView* S, const WfState& W, int slot, int light, V3
 }
 
 /* one shade of a vol_path slot */
-DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, unsigned long long* stats, bool counting) {
+DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting) {
     const WfJob& J = W.jobs[W.job[slot]];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;
@@ -769,9 +783,7 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
         }
         if (fl & (F_WTR | F_WIT)) {
             W.flags[slot] = fl;
-            const int a = warp_append(&W.ctr->n_active[next], true);
-            set_active(W, next, a, slot);
-            return;
+            return true;
         }
     }
     float4 cf = W.coeff[slot], rdv = W.rad[slot];
@@ -990,20 +1002,14 @@ DF void shade_vol_path(const WfState& W, int slot, int next, uint32_t* status, u
     W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
     if (ext || (fl & (F_WTR | F_WIT))) {
         W.flags[slot] = fl;
-        const int a = warp_append(&W.ctr->n_active[next], true);
-        set_active(W, next, a, slot);
-        return;
+        return true;
     }
     /* the path is over */
     finish_path(J, W, slot, radiance, stats, WF_PASS_RENDER);
     if (counting) warp_add64(stats + 0, 1u);
-    if (start_path(W, slot, true)) {
-        const int a = warp_append(&W.ctr->n_active[next], true);
-        set_active(W, next, a, slot);
-    } else {
-        W.flags[slot] = 0;
-        warp_append(&W.ctr->n_active[next], false);
-    }
+    if (start_path(W, slot, true)) return true;
+    W.flags[slot] = 0;
+    return false;
 }
 
 __global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
@@ -1011,7 +1017,11 @@ __global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState 
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) shade_vol_path(W, sorted ? W.sorted[i] : W.active[cur][i], cur ^ 1, status, stats, counting);
+    int slot = -1;
+    bool keep = false;
+    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; keep = shade_vol_path(W, slot, status, stats, counting); }
+    const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
+    if (keep) set_active(W, cur ^ 1, a, slot);
 }
 
 /* the active paths of this iteration, one thread each over the sorted list
@@ -1034,7 +1044,11 @@ __global__ void __launch_bounds__(128, (kAdj || kDynamic) ? 5 : RT_SHADE_BLOCKS)
     list = sorted ? W.sorted : W.active[cur];
     if (!kDynamic) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < n) shade_path<kAdj>(W, list[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+        int slot = -1;
+        bool keep = false;
+        if (i < n) { slot = list[i]; keep = shade_path<kAdj>(W, slot, status, stats, counting, pass, A, s_alpha); }
+        const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
+        if (keep) set_active(W, cur ^ 1, a, slot);
     } else {
         const int lane = threadIdx.x & 31;
         while (true) {
@@ -1043,8 +1057,12 @@ __global__ void __launch_bounds__(128, (kAdj || kDynamic) ? 5 : RT_SHADE_BLOCKS)
             base = __shfl_sync(kFullWarp, base, 0);
             if (base >= n) break;
             const int i = base + lane;
-            if (i < n) shade_path<kAdj>(W, list[i], cur ^ 1, status, stats, counting, pass, A, s_alpha);
+            int slot = -1;
+            bool keep = false;
+            if (i < n) { slot = list[i]; keep = shade_path<kAdj>(W, slot, status, stats, counting, pass, A, s_alpha); }
             __syncwarp();
+            const int a = warp_append(&W.ctr->n_active[cur ^ 1], keep);
+            if (keep) set_active(W, cur ^ 1, a, slot);
         }
     }
     if (kAdj) {
@@ -1118,7 +1136,9 @@ __global__ void __launch_bounds__(256) k_wf_start_particles(WfState W) {
     start_particle(W, slot);
 }
 
-DF void shade_particle(const WfState& W, int slot, int next, uint32_t* status) {
+/* returns whether the slot holds a particle for the next iteration (the caller appends it
+ * to the next active list) */
+DF bool shade_particle(const WfState& W, int slot, uint32_t* status) {
     const WfJob& J = W.jobs[0];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;
@@ -1189,13 +1209,9 @@ DF void shade_particle(const WfState& W, int slot, int next, uint32_t* status) {
     }
     if (!(fl & F_DONE)) {
         W.flags[slot] = fl;
-        const int a = warp_append(&W.ctr->n_active[next], true);
-        set_active(W, next, a, slot);
-        return;
+        return true;
     }
-    const bool more = start_particle(W, slot);
-    const int a = warp_append(&W.ctr->n_active[next], more);
-    if (more) set_active(W, next, a, slot);
+    return start_particle(W, slot);
 }
 
 /* `sorted`: the list regrouped by shade key, else the active list as built
@@ -1204,7 +1220,11 @@ __global__ void __launch_bounds__(128, RT_PSHADE_BLOCKS) k_wf_shade_particle(WfS
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) shade_particle(W, sorted ? W.sorted[i] : W.active[cur][i], cur ^ 1, status);
+    int slot = -1;
+    bool keep = false;
+    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; keep = shade_particle(W, slot, status); }
+    const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
+    if (keep) set_active(W, cur ^ 1, a, slot);
 }
 
 __global__ void k_wf_active_init(WfState W) {
