@@ -92,6 +92,30 @@ DF int block_append(int* counter, bool want) {
     return r;
 }
 
+/* Three block-aggregated appends in one pass (one atomic per counter per
+ * block, the three in flight together); same calling rule as block_append. */
+DF void block_append3(int* c0, bool w0, int* c1, bool w1, int* c2, bool w2, int* r0, int* r1, int* r2) {
+    __shared__ int s_cnt[3][32];
+    __shared__ int s_base[3];
+    const unsigned b0 = __ballot_sync(0xffffffffu, w0), b1 = __ballot_sync(0xffffffffu, w1),
+                   b2 = __ballot_sync(0xffffffffu, w2);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) { s_cnt[0][w] = __popc(b0); s_cnt[1][w] = __popc(b1); s_cnt[2][w] = __popc(b2); }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int* c = threadIdx.x == 0 ? c0 : (threadIdx.x == 1 ? c1 : c2);
+        int t = 0;
+        for (int k = 0; k < nw; k++) { const int v = s_cnt[threadIdx.x][k]; s_cnt[threadIdx.x][k] = t; t += v; }
+        s_base[threadIdx.x] = t ? atomicAdd(c, t) : 0;
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    *r0 = w0 ? s_base[0] + s_cnt[0][w] + __popc(b0 & lt) : -1;
+    *r1 = w1 ? s_base[1] + s_cnt[1][w] + __popc(b1 & lt) : -1;
+    *r2 = w2 ? s_base[2] + s_cnt[2][w] + __popc(b2 & lt) : -1;
+    __syncthreads();
+}
+
 /* Debug-bounds builds (-DRT_DEBUG_BOUNDS) check every computed index into a
  * path-state buffer: one outside its buffer sets RT_STATUS_BOUNDS and the
  * access is skipped (no trap), so the host reports RT_ERR_BOUNDS. */
@@ -106,6 +130,13 @@ DF bool in_bounds(const WfState&, long long, long long) { return true; }
 #endif
 DF void set_active(const WfState& W, int list, int a, int slot) {
     if (in_bounds(W, a, W.slots)) W.active[list][a] = slot;
+}
+
+DF void push_ray4(const WfState& W, int q, int path, int kind, float4 o, float4 d) {
+    if (!in_bounds(W, q, 3LL * W.slots)) return;
+    W.q_o[q] = o;
+    W.q_d[q] = d;
+    W.q_meta[q] = (path << 10) | ((int)W.job[path] << 2) | kind;
 }
 
 DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
@@ -1095,16 +1126,30 @@ DF bool particle_continue(const RtParams& P, int bounces, C3* coeff, Rng& rand) 
     return true;
 }
 
-/* Claims particles for `slot` until one has an extension ray to trace (a
- * particle can end before its first ray: no light, black emission, depth
- * limit or roulette).  false once every particle of the round is claimed. */
-DF bool start_particle(const WfState& W, int slot) {
+/* What a light-tracer shade leaves for the queues: the camera connection's
+ * splat ray, the next extension ray, and whether the slot holds a particle
+ * for the next iteration.  The kernel appends them for the whole block. */
+struct PartOut {
+    float4 so, sd, eo, ed;
+    bool splat, ext, keep;
+};
+
+DF void ray4(const Ray& r, float4* o, float4* d) {
+    *o = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
+    *d = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
+}
+
+/* Claims particles for `slot`, the first one `sid` (claimed by the caller),
+ * until one has an extension ray to trace (a particle can end before its
+ * first ray: no light, black emission, depth limit or roulette).  The ray
+ * goes to `o`; o->keep is false once every particle of the round is claimed. */
+DF void start_particle(const WfState& W, int slot, long long sid, PartOut* o) {
     const WfJob& J = W.jobs[0];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;
-    while (true) {
-        const long long sid = (long long)atomicAdd(&W.ctr->next_sample, 1ull);
-        if (sid >= W.ctr->total) { W.flags[slot] = 0; return false; }
+    for (bool first = true;; first = false) {
+        if (!first) sid = (long long)atomicAdd(&W.ctr->next_sample, 1ull);
+        if (sid >= W.ctr->total) { W.flags[slot] = 0; o->keep = false; return; }
         const long long i = J.first + sid;
         Rng rand;
         rng_init(rand, P.seed, (uint32_t)(uint64_t)i, (uint32_t)((uint64_t)i >> 32), RT_PARTICLE_STREAM);
@@ -1122,23 +1167,52 @@ DF bool start_particle(const WfState& W, int slot) {
         W.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.0f);
         W.bounce[slot] = make_int2(1, 1);
         W.flags[slot] = F_ALIVE | F_EXT;
-        W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
-        W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
-        const int q = warp_append(&W.ctr->n_closest, true);
-        push_ray(W, q, slot, WF_RAY_EXT, ray);
-        return true;
+        ray4(ray, &o->eo, &o->ed);
+        W.ray_o[slot] = o->eo;
+        W.ray_d[slot] = o->ed;
+        o->ext = true;
+        o->keep = true;
+        return;
     }
+}
+
+/* The warp's lanes with `want` claim consecutive particle ids with one atomic;
+ * -1 for the others.  Every lane of the warp calls it. */
+DF long long claim_particle(const WfState& W, bool want) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return -1;
+    const int leader = __ffs(m) - 1, lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&W.ctr->next_sample, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return want ? (long long)base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+/* queue the block's splat and extension rays and its next active slots */
+DF void particle_queues(const WfState& W, int slot, int next, const PartOut& o) {
+    int qs, qe, a;
+    block_append3(&W.ctr->n_shadow, o.splat, &W.ctr->n_closest, o.ext, &W.ctr->n_active[next], o.keep, &qs, &qe, &a);
+    if (o.splat) push_ray4(W, W.shadow_base + qs, slot, WF_RAY_SPLAT, o.so, o.sd);
+    if (o.ext) push_ray4(W, qe, slot, WF_RAY_EXT, o.eo, o.ed);
+    if (o.keep) set_active(W, next, a, slot);
 }
 
 __global__ void __launch_bounds__(256) k_wf_start_particles(WfState W) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= W.slots) return;
-    start_particle(W, slot);
+    PartOut o;
+    o.splat = o.ext = o.keep = false;
+    const bool in = slot < W.slots;
+    const long long sid = claim_particle(W, in);
+    if (in) start_particle(W, slot, sid, &o);
+    /* the first active list is built from the slots' flags afterwards */
+    int qs, qe, a;
+    block_append3(&W.ctr->n_shadow, false, &W.ctr->n_closest, o.ext, &W.ctr->n_active[0], false, &qs, &qe, &a);
+    if (o.ext) push_ray4(W, qe, slot, WF_RAY_EXT, o.eo, o.ed);
 }
 
-/* returns whether the slot holds a particle for the next iteration (the caller appends it
- * to the next active list) */
-DF bool shade_particle(const WfState& W, int slot, uint32_t* status) {
+/* One vertex of the slot's particle; its rays go to `o`.  Returns true when
+ * the particle is over (the caller starts the next one in the slot). */
+DF bool shade_particle(const WfState& W, int slot, uint32_t* status, PartOut* o) {
     const WfJob& J = W.jobs[0];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;
@@ -1179,8 +1253,8 @@ DF bool shade_particle(const WfState& W, int slot, uint32_t* status) {
                                 pix = x * S->camera.height + y;
                         }
                         W.pd_l1[slot] = make_float4(color.r, color.g, color.b, __int_as_float(pix));
-                        const int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
-                        push_ray(W, q, slot, WF_RAY_SPLAT, mkray(cw.pos, Normalize(vec), 0.0001f, dis - 0.0001f));
+                        ray4(mkray(cw.pos, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
+                        o->splat = true;
                     }
                 }
                 const BSample bs = MatSample<true>(S, mat, wo, it.UV, rand);
@@ -1197,10 +1271,10 @@ DF bool shade_particle(const WfState& W, int slot, uint32_t* status) {
             ext = true;
         } while (false);
         if (ext) {
-            const int q = warp_append(&W.ctr->n_closest, true);
-            push_ray(W, q, slot, WF_RAY_EXT, nray);
-            W.ray_o[slot] = make_float4(nray.O.x, nray.O.y, nray.O.z, nray.MinT);
-            W.ray_d[slot] = make_float4(nray.D.x, nray.D.y, nray.D.z, nray.MaxT);
+            ray4(nray, &o->eo, &o->ed);
+            o->ext = true;
+            W.ray_o[slot] = o->eo;
+            W.ray_d[slot] = o->ed;
         }
         W.bounce[slot] = make_int2(bounces, guard);
         W.rng_n[slot] = rand.n;
@@ -1209,9 +1283,10 @@ DF bool shade_particle(const WfState& W, int slot, uint32_t* status) {
     }
     if (!(fl & F_DONE)) {
         W.flags[slot] = fl;
-        return true;
+        o->keep = true;
+        return false;
     }
-    return start_particle(W, slot);
+    return true;
 }
 
 /* `sorted`: the list regrouped by shade key, else the active list as built
@@ -1221,10 +1296,14 @@ __global__ void __launch_bounds__(128, RT_PSHADE_BLOCKS) k_wf_shade_particle(WfS
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int slot = -1;
-    bool keep = false;
-    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; keep = shade_particle(W, slot, status); }
-    const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
-    if (keep) set_active(W, cur ^ 1, a, slot);
+    PartOut o;
+    o.splat = o.ext = o.keep = false;
+    bool restart = false;
+    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; restart = shade_particle(W, slot, status, &o); }
+    /* a finished particle's slot takes the next particle at once */
+    const long long sid = claim_particle(W, restart);
+    if (restart) start_particle(W, slot, sid, &o);
+    particle_queues(W, slot, cur ^ 1, o);
 }
 
 __global__ void k_wf_active_init(WfState W) {
