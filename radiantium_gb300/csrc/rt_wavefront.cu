@@ -92,28 +92,50 @@ DF int block_append(int* counter, bool want) {
     return r;
 }
 
-/* Three block-aggregated appends in one pass (one atomic per counter per
- * block, the three in flight together); same calling rule as block_append. */
-DF void block_append3(int* c0, bool w0, int* c1, bool w1, int* c2, bool w2, int* r0, int* r1, int* r2) {
-    __shared__ int s_cnt[3][32];
-    __shared__ int s_base[3];
-    const unsigned b0 = __ballot_sync(0xffffffffu, w0), b1 = __ballot_sync(0xffffffffu, w1),
-                   b2 = __ballot_sync(0xffffffffu, w2);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0) { s_cnt[0][w] = __popc(b0); s_cnt[1][w] = __popc(b1); s_cnt[2][w] = __popc(b2); }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        int* c = threadIdx.x == 0 ? c0 : (threadIdx.x == 1 ? c1 : c2);
-        int t = 0;
-        for (int k = 0; k < nw; k++) { const int v = s_cnt[threadIdx.x][k]; s_cnt[threadIdx.x][k] = t; t += v; }
-        s_base[threadIdx.x] = t ? atomicAdd(c, t) : 0;
+/* Appends a shade's rays and its slot for the next iteration in one pass:
+ * the shadow queue, the closest-hit queue (the warp's MIS rays, then its
+ * extension rays) and the next active list `next`.  kBlock: one atomic per
+ * counter per block, every thread of the block calls it (blockDim.x a
+ * multiple of 32); else one per warp, every lane of the warp calls it.  The
+ * three counters' atomics are in flight together.  Outputs are queue
+ * positions (the shadow one including shadow_base), -1 where not wanted. */
+template <bool kBlock>
+DF void queue_append(const WfState& W, int next, bool shadow, bool mis, bool ext, bool keep,
+                     int* qs, int* qm, int* qe, int* qa) {
+    const unsigned full = 0xffffffffu;
+    const unsigned bs = __ballot_sync(full, shadow), bm = __ballot_sync(full, mis),
+                   be = __ballot_sync(full, ext), ba = __ballot_sync(full, keep);
+    const int lane = threadIdx.x & 31;
+    int b0, b1, b2;
+    if (kBlock) {
+        __shared__ int s_cnt[3][32];
+        __shared__ int s_base[3];
+        const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if (lane == 0) { s_cnt[0][w] = __popc(bs); s_cnt[1][w] = __popc(bm) + __popc(be); s_cnt[2][w] = __popc(ba); }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            int* c = threadIdx.x == 0 ? &W.ctr->n_shadow : (threadIdx.x == 1 ? &W.ctr->n_closest : &W.ctr->n_active[next]);
+            int t = 0;
+            for (int k = 0; k < nw; k++) { const int v = s_cnt[threadIdx.x][k]; s_cnt[threadIdx.x][k] = t; t += v; }
+            s_base[threadIdx.x] = t ? atomicAdd(c, t) : 0;
+        }
+        __syncthreads();
+        b0 = s_base[0] + s_cnt[0][w]; b1 = s_base[1] + s_cnt[1][w]; b2 = s_base[2] + s_cnt[2][w];
+        __syncthreads();
+    } else {
+        int v = 0;
+        if (lane < 3) {
+            const int t = lane == 0 ? __popc(bs) : (lane == 1 ? __popc(bm) + __popc(be) : __popc(ba));
+            int* c = lane == 0 ? &W.ctr->n_shadow : (lane == 1 ? &W.ctr->n_closest : &W.ctr->n_active[next]);
+            if (t) v = atomicAdd(c, t);
+        }
+        b0 = __shfl_sync(full, v, 0); b1 = __shfl_sync(full, v, 1); b2 = __shfl_sync(full, v, 2);
     }
-    __syncthreads();
     const unsigned lt = (1u << lane) - 1u;
-    *r0 = w0 ? s_base[0] + s_cnt[0][w] + __popc(b0 & lt) : -1;
-    *r1 = w1 ? s_base[1] + s_cnt[1][w] + __popc(b1 & lt) : -1;
-    *r2 = w2 ? s_base[2] + s_cnt[2][w] + __popc(b2 & lt) : -1;
-    __syncthreads();
+    *qs = shadow ? W.shadow_base + b0 + __popc(bs & lt) : -1;
+    *qm = mis ? b1 + __popc(bm & lt) : -1;
+    *qe = ext ? b1 + __popc(bm) + __popc(be & lt) : -1;
+    *qa = keep ? b2 + __popc(ba & lt) : -1;
 }
 
 /* Debug-bounds builds (-DRT_DEBUG_BOUNDS) check every computed index into a
@@ -137,6 +159,11 @@ DF void push_ray4(const WfState& W, int q, int path, int kind, float4 o, float4 
     W.q_o[q] = o;
     W.q_d[q] = d;
     W.q_meta[q] = (path << 10) | ((int)W.job[path] << 2) | kind;
+}
+
+DF void ray4(const Ray& r, float4* o, float4* d) {
+    *o = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
+    *d = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
 }
 
 DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
@@ -180,22 +207,24 @@ DF void sample_pixel(const RtParams& P, int64_t sid, int* lx, int* ly, int* k) {
     *ly = band * 4 + rr % bh;
 }
 
-/* initialises a camera sample in `slot` and enqueues its first ray; the
- * warp claims its sample ids with one atomic.  Returns false (slot emptied)
- * when every sample of the round has been started. */
-DF bool start_path(const WfState& W, int slot, bool take) {
-    const long long total = W.ctr->total;
-    unsigned mask = __ballot_sync(__activemask(), take);
-    long long sid = -1;
-    if (take) {
-        int leader = __ffs(mask) - 1, lane = threadIdx.x & 31;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&W.ctr->next_sample, (unsigned long long)__popc(mask));
-        base = __shfl_sync(mask, base, leader);
-        long long id = (long long)base + __popc(mask & ((1u << lane) - 1u));
-        if (id < total) sid = id;
-    }
-    int q = warp_append(&W.ctr->n_closest, sid >= 0);
+/* The lanes of `active` with `want` claim consecutive sample ids with one
+ * atomic; -1 for the others and for ids past the round's end.  Every lane of
+ * `active` calls it. */
+DF long long claim_sample(const WfState& W, unsigned active, bool want) {
+    const unsigned m = __ballot_sync(active, want);
+    if (!want) return -1;
+    const int leader = __ffs(m) - 1, lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&W.ctr->next_sample, (unsigned long long)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    const long long id = (long long)base + __popc(m & ((1u << lane) - 1u));
+    return id < W.ctr->total ? id : -1;
+}
+
+/* Initialises camera sample `sid` in `slot`; its first ray goes to W.ray_o /
+ * ray_d and to (o, d).  sid < 0 empties the slot.  Returns whether a path
+ * started. */
+DF bool init_path(const WfState& W, int slot, long long sid, float4* o, float4* d) {
     if (sid < 0) { W.flags[slot] = 0; return false; }
     const int j = job_of(W, sid);
     const WfJob& J = W.jobs[j];
@@ -215,16 +244,33 @@ DF bool start_path(const WfState& W, int slot, bool take) {
     W.bounce[slot] = make_int2(0, 0);
     W.flags[slot] = F_ALIVE | F_SPECULAR | F_EXT;
     W.vol_env[slot] = J.view->global_medium;
-    W.ray_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
-    W.ray_d[slot] = make_float4(ray.D.x, ray.D.y, ray.D.z, ray.MaxT);
-    push_ray(W, q, slot, WF_RAY_EXT, ray);
+    ray4(ray, o, d);
+    W.ray_o[slot] = *o;
+    W.ray_d[slot] = *d;
+    return true;
+}
+
+/* A finished path's slot takes the next camera sample and enqueues its first
+ * ray (the warp's active lanes claim their ids with one atomic).  Returns
+ * false (slot emptied) when every sample of the round has been started. */
+DF bool start_path(const WfState& W, int slot, bool take) {
+    const long long sid = claim_sample(W, __activemask(), take);
+    const int q = warp_append(&W.ctr->n_closest, sid >= 0);
+    float4 o, d;
+    if (!init_path(W, slot, sid, &o, &d)) return false;
+    push_ray4(W, q, slot, WF_RAY_EXT, o, d);
     return true;
 }
 
 __global__ void __launch_bounds__(256) k_wf_start(WfState W) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= W.slots) return;
-    start_path(W, slot, true);
+    const bool in = slot < W.slots;
+    const long long sid = claim_sample(W, 0xffffffffu, in);
+    float4 o, d;
+    const bool ok = in && init_path(W, slot, sid, &o, &d);
+    int qs, qm, qe, qa;
+    queue_append<true>(W, 0, false, false, ok, false, &qs, &qm, &qe, &qa);
+    if (ok) push_ray4(W, qe, slot, WF_RAY_EXT, o, d);
 }
 
 /* Persistent traversal with dynamic ray fetch (Aila & Laine 2009): each warp
@@ -451,8 +497,17 @@ DF void finish_path(const WfJob& J, const WfState& W, int slot, C3 rad, unsigned
 
 /* one bounce of PathTracer.Mis / NextEventEstimation / OnlySampleBxdf after the
  * extension hit is known (PathTracer.cs:43-270) */
+/* What a path shade leaves for the queues: its shadow ray, whether it
+ * queued a MIS ray (in pd_ray_o / pd_ray_d) or an extension ray (in ray_o /
+ * ray_d), whether the slot stays active, and whether the path is over (the
+ * caller starts the next camera sample in the slot). */
+struct PathOut {
+    float4 so, sd;
+    bool shadow, mis, ext, keep, restart;
+};
+
 template <bool kAdj>
-DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting,
+DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting,
                    int pass, const WfAdjoint& A, float* s_alpha) {
     const WfJob& J = W.jobs[W.job[slot]];
     const RtSceneView* S = J.view;
@@ -593,8 +648,8 @@ DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long l
                                     C3 l1 = fr * ls.Li * weight / ls.Pdf;
                                     W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
                                     fl |= F_L1;
-                                    int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
-                                    push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
+                                    ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
+                                    o->shadow = true;
                                 }
                             }
                         }
@@ -622,8 +677,7 @@ DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long l
                                 W.pd_ray_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
                                 W.pd_ray_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, toLight.MaxT);
                                 fl |= F_L2;
-                                int q = warp_append(&W.ctr->n_closest, true);
-                                push_ray(W, q, slot, WF_RAY_MIS, toLight);
+                                o->mis = true;
                             }
                         }
                     } else {
@@ -643,8 +697,8 @@ DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long l
                                 C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
                                 W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
                                 zero = false;
-                                int q = W.shadow_base + warp_append(&W.ctr->n_shadow, true);
-                                push_ray(W, q, slot, WF_RAY_SHADOW, mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f));
+                                ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
+                                o->shadow = true;
                             }
                         }
                         if (zero) fl |= F_DZERO;
@@ -675,10 +729,9 @@ DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long l
             ext = true;
         } while (false);
         if (ext) {
-            int q = warp_append(&W.ctr->n_closest, true);
-            push_ray(W, q, slot, WF_RAY_EXT, nray);
             W.ray_o[slot] = make_float4(nray.O.x, nray.O.y, nray.O.z, nray.MinT);
             W.ray_d[slot] = make_float4(nray.D.x, nray.D.y, nray.D.z, nray.MaxT);
+            o->ext = true;
         }
         W.bounce[slot] = make_int2(bounces, guard);
         W.rng_n[slot] = rand.n;
@@ -690,13 +743,30 @@ DF bool shade_path(const WfState& W, int slot, uint32_t* status, unsigned long l
     /* the slot stays active while it waits for rays */
     if ((fl & F_PENDING) || !(fl & F_DONE)) {
         W.flags[slot] = fl;
-        return true;
+        o->keep = true;
+        return;
     }
     finish_path(J, W, slot, radiance, stats, pass);
     if (counting) warp_add64(stats + 0, 1u);
-    if (start_path(W, slot, true)) return true;
-    W.flags[slot] = 0;
-    return false;
+    o->restart = true;
+}
+
+/* The shade's queue appends, for the block (kBlock) or the warp: a finished
+ * path's slot takes the next camera sample at once. */
+template <bool kBlock>
+DF void path_queues(const WfState& W, int slot, int next, PathOut& o) {
+    const long long sid = claim_sample(W, 0xffffffffu, o.restart);
+    float4 ro, rd;
+    if (o.restart && init_path(W, slot, sid, &ro, &rd)) { o.ext = true; o.keep = true; }
+    int qs, qm, qe, qa;
+    queue_append<kBlock>(W, next, o.shadow, o.mis, o.ext, o.keep, &qs, &qm, &qe, &qa);
+    if (o.shadow) push_ray4(W, qs, slot, WF_RAY_SHADOW, o.so, o.sd);
+    if (o.mis) push_ray4(W, qm, slot, WF_RAY_MIS, W.pd_ray_o[slot], W.pd_ray_d[slot]);
+    if (o.ext) {
+        if (!o.restart) { ro = W.ray_o[slot]; rd = W.ray_d[slot]; }
+        push_ray4(W, qe, slot, WF_RAY_EXT, ro, rd);
+    }
+    if (o.keep) set_active(W, next, qa, slot);
 }
 
 /* ---- vol_path (VolumetricPathTracer.Li, Integrators/VolumetricPathTracer.cs) ----
@@ -1076,10 +1146,10 @@ __global__ void __launch_bounds__(128, (kAdj || kDynamic) ? 5 : RT_SHADE_BLOCKS)
     if (!kDynamic) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         int slot = -1;
-        bool keep = false;
-        if (i < n) { slot = list[i]; keep = shade_path<kAdj>(W, slot, status, stats, counting, pass, A, s_alpha); }
-        const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
-        if (keep) set_active(W, cur ^ 1, a, slot);
+        PathOut o;
+        o.shadow = o.mis = o.ext = o.keep = o.restart = false;
+        if (i < n) { slot = list[i]; shade_path<kAdj>(&o, W, slot, status, stats, counting, pass, A, s_alpha); }
+        path_queues<true>(W, slot, cur ^ 1, o);
     } else {
         const int lane = threadIdx.x & 31;
         while (true) {
@@ -1089,11 +1159,11 @@ __global__ void __launch_bounds__(128, (kAdj || kDynamic) ? 5 : RT_SHADE_BLOCKS)
             if (base >= n) break;
             const int i = base + lane;
             int slot = -1;
-            bool keep = false;
-            if (i < n) { slot = list[i]; keep = shade_path<kAdj>(W, slot, status, stats, counting, pass, A, s_alpha); }
+            PathOut o;
+            o.shadow = o.mis = o.ext = o.keep = o.restart = false;
+            if (i < n) { slot = list[i]; shade_path<kAdj>(&o, W, slot, status, stats, counting, pass, A, s_alpha); }
             __syncwarp();
-            const int a = warp_append(&W.ctr->n_active[cur ^ 1], keep);
-            if (keep) set_active(W, cur ^ 1, a, slot);
+            path_queues<false>(W, slot, cur ^ 1, o);
         }
     }
     if (kAdj) {
@@ -1133,11 +1203,6 @@ struct PartOut {
     float4 so, sd, eo, ed;
     bool splat, ext, keep;
 };
-
-DF void ray4(const Ray& r, float4* o, float4* d) {
-    *o = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
-    *d = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
-}
 
 /* Claims particles for `slot`, the first one `sid` (claimed by the caller),
  * until one has an extension ray to trace (a particle can end before its
@@ -1190,9 +1255,9 @@ DF long long claim_particle(const WfState& W, bool want) {
 
 /* queue the block's splat and extension rays and its next active slots */
 DF void particle_queues(const WfState& W, int slot, int next, const PartOut& o) {
-    int qs, qe, a;
-    block_append3(&W.ctr->n_shadow, o.splat, &W.ctr->n_closest, o.ext, &W.ctr->n_active[next], o.keep, &qs, &qe, &a);
-    if (o.splat) push_ray4(W, W.shadow_base + qs, slot, WF_RAY_SPLAT, o.so, o.sd);
+    int qs, qm, qe, a;
+    queue_append<true>(W, next, o.splat, false, o.ext, o.keep, &qs, &qm, &qe, &a);
+    if (o.splat) push_ray4(W, qs, slot, WF_RAY_SPLAT, o.so, o.sd);
     if (o.ext) push_ray4(W, qe, slot, WF_RAY_EXT, o.eo, o.ed);
     if (o.keep) set_active(W, next, a, slot);
 }
@@ -1205,8 +1270,8 @@ __global__ void __launch_bounds__(256) k_wf_start_particles(WfState W) {
     const long long sid = claim_particle(W, in);
     if (in) start_particle(W, slot, sid, &o);
     /* the first active list is built from the slots' flags afterwards */
-    int qs, qe, a;
-    block_append3(&W.ctr->n_shadow, false, &W.ctr->n_closest, o.ext, &W.ctr->n_active[0], false, &qs, &qe, &a);
+    int qs, qm, qe, a;
+    queue_append<true>(W, 0, false, false, o.ext, false, &qs, &qm, &qe, &a);
     if (o.ext) push_ray4(W, qe, slot, WF_RAY_EXT, o.eo, o.ed);
 }
 
