@@ -72,26 +72,6 @@ DF int warp_append(int* counter, bool want) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
-/* Block-aggregated append: one atomic per block.  Every thread of the block
- * calls it (blockDim.x a multiple of 32, at most 1024). */
-DF int block_append(int* counter, bool want) {
-    __shared__ int s_cnt[32];
-    __shared__ int s_base;
-    const unsigned b = __ballot_sync(0xffffffffu, want);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0) s_cnt[w] = __popc(b);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int t = 0;
-        for (int k = 0; k < nw; k++) { const int c = s_cnt[k]; s_cnt[k] = t; t += c; }
-        s_base = t ? atomicAdd(counter, t) : 0;
-    }
-    __syncthreads();
-    const int r = want ? s_base + s_cnt[w] + __popc(b & ((1u << lane) - 1u)) : -1;
-    __syncthreads();
-    return r;
-}
-
 /* Appends a shade's rays and its slot for the next iteration in one pass:
  * the shadow queue, the closest-hit queue (the warp's MIS rays, then its
  * extension rays) and the next active list `next`.  kBlock: one atomic per
@@ -247,18 +227,6 @@ DF bool init_path(const WfState& W, int slot, long long sid, float4* o, float4* 
     ray4(ray, o, d);
     W.ray_o[slot] = *o;
     W.ray_d[slot] = *d;
-    return true;
-}
-
-/* A finished path's slot takes the next camera sample and enqueues its first
- * ray (the warp's active lanes claim their ids with one atomic).  Returns
- * false (slot emptied) when every sample of the round has been started. */
-DF bool start_path(const WfState& W, int slot, bool take) {
-    const long long sid = claim_sample(W, __activemask(), take);
-    const int q = warp_append(&W.ctr->n_closest, sid >= 0);
-    float4 o, d;
-    if (!init_path(W, slot, sid, &o, &d)) return false;
-    push_ray4(W, q, slot, WF_RAY_EXT, o, d);
     return true;
 }
 
@@ -784,15 +752,18 @@ DF int pack_env(int env, int count) { return (count << 16) | ((env + 1) & 0xFFFF
 DF int env_of(int packed) { return (packed & 0xFFFF) - 1; }
 DF int count_of(int packed) { return packed >> 16; }
 
-/* next Transmittance segment from the walk's current start; false: walk over */
-DF bool trw_push(const WfState& W, int slot) {
+/* the next Transmittance segment from the walk's current start (o, d); false: the walk is over */
+DF bool trw_ray(const WfState& W, int slot, float4* o, float4* d) {
     const float4 st = W.trw_start[slot], en = W.trw_end[slot], dr = W.trw_dir[slot];
     const V3 start = v3(st.x, st.y, st.z), to = v3(en.x, en.y, en.z);
     const float dis = Length(to - start);
     if (dis < 0.0001f) return false;
-    const int q = warp_append(&W.ctr->n_closest, true);
-    push_ray(W, q, slot, WF_RAY_TRW, mkray(start, v3(dr.x, dr.y, dr.z), 0.0001f, dis - 0.0001f));
+    ray4(mkray(start, v3(dr.x, dr.y, dr.z), 0.0001f, dis - 0.0001f), o, d);
     return true;
+}
+DF bool trw_next(const WfState& W, int slot) {
+    float4 o, d;
+    return trw_ray(W, slot, &o, &d);
 }
 /* Scene.Transmittance (Scene.cs:72-103), one traced segment; true: continues */
 DF bool trw_step(const RtSceneView* S, const WfState& W, int slot) {
@@ -821,11 +792,7 @@ DF bool trw_step(const RtSceneView* S, const WfState& W, int slot) {
     if (!more) return false;
     W.trw_start[slot] = make_float4(start.x, start.y, start.z, __int_as_float(env));
     W.trw_end[slot] = make_float4(to.x, to.y, to.z, __int_as_float(count));
-    return trw_push(W, slot);
-}
-DF void itw_push(const WfState& W, int slot, const Ray& r) {
-    const int q = warp_append(&W.ctr->n_closest, true);
-    push_ray(W, q, slot, WF_RAY_MIS, r);
+    return trw_next(W, slot);
 }
 /* Scene.IntersectTr (Scene.cs:105-131), one traced segment; true: continues.
  * When over, itw_o holds the radiance found (light-identity check of
@@ -861,7 +828,6 @@ DF bool itw_step(const RtSceneView* S, const WfState& W, int slot, int light, V3
     if (more) {
         W.itw_o[slot] = make_float4(ray.O.x, ray.O.y, ray.O.z, ray.MinT);
         W.itw_tr[slot] = make_float4(tr.r, tr.g, tr.b, __int_as_float(pack_env(env, count)));
-        itw_push(W, slot, ray);
         return true;
     }
     W.itw_o[slot] = make_float4(li.r, li.g, li.b, 0.0f);
@@ -869,8 +835,17 @@ DF bool itw_step(const RtSceneView* S, const WfState& W, int slot, int light, V3
     return false;
 }
 
+/* What a vol_path shade leaves for the queues: a Transmittance segment
+ * (its ray rebuilt from trw_*), an IntersectTr segment (from itw_*) or the
+ * extension ray (ray_o / ray_d), whether the slot stays active, whether the
+ * path is over.  A shade starts walk segments or an extension ray, never both. */
+struct VolOut {
+    bool trw, itw, ext, keep, restart;
+};
+
 /* one shade of a vol_path slot */
-DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting) {
+DF void shade_vol_path(VolOut* o, const WfState& W, int slot, uint32_t* status, unsigned long long* stats,
+                       bool counting) {
     const WfJob& J = W.jobs[W.job[slot]];
     const RtSceneView* S = J.view;
     const RtParams P = J.P;
@@ -884,7 +859,10 @@ DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned lo
         }
         if (fl & (F_WTR | F_WIT)) {
             W.flags[slot] = fl;
-            return true;
+            o->trw = (fl & F_WTR) != 0;
+            o->itw = (fl & F_WIT) != 0;
+            o->keep = true;
+            return;
         }
     }
     float4 cf = W.coeff[slot], rdv = W.rad[slot];
@@ -915,9 +893,6 @@ DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned lo
         if (fl & F_DONE) break;
         if (fl & F_CONT) {                       /* 3. the continuation sampled with the term */
             fl &= ~F_CONT;
-            const float4 ro = W.ray_o[slot], rd = W.ray_d[slot];
-            const int q = warp_append(&W.ctr->n_closest, true);
-            push_ray(W, q, slot, WF_RAY_EXT, mkray(v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), ro.w, rd.w));
             ext = true;
             break;
         }
@@ -1091,11 +1066,7 @@ DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned lo
         fl = (fl & ~F_SPECULAR) | (isSpecularPath ? F_SPECULAR : 0u);
         /* start the walks of the new direct term; if there are none, resolve it now */
         if (fl & F_WTR) {
-            if (!trw_push(W, slot)) fl &= ~F_WTR;
-        }
-        if (fl & F_WIT) {
-            const float4 o = W.itw_o[slot], d = W.itw_d[slot];
-            itw_push(W, slot, mkray(v3(o.x, o.y, o.z), v3(d.x, d.y, d.z), o.w));
+            if (!trw_next(W, slot)) fl &= ~F_WTR;
         }
         if (fl & (F_WTR | F_WIT)) break;
     }
@@ -1103,14 +1074,41 @@ DF bool shade_vol_path(const WfState& W, int slot, uint32_t* status, unsigned lo
     W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0.0f);
     if (ext || (fl & (F_WTR | F_WIT))) {
         W.flags[slot] = fl;
-        return true;
+        o->trw = (fl & F_WTR) != 0;
+        o->itw = (fl & F_WIT) != 0;
+        o->ext = ext;
+        o->keep = true;
+        return;
     }
     /* the path is over */
     finish_path(J, W, slot, radiance, stats, WF_PASS_RENDER);
     if (counting) warp_add64(stats + 0, 1u);
-    if (start_path(W, slot, true)) return true;
-    W.flags[slot] = 0;
-    return false;
+    o->restart = true;
+}
+
+/* The vol_path shade's queue appends for the block: a Transmittance segment
+ * takes the first closest-hit position of the lane, an IntersectTr segment or
+ * the extension ray the second; a finished path's slot takes the next camera
+ * sample at once. */
+DF void vol_queues(const WfState& W, int slot, int next, VolOut& o) {
+    const long long sid = claim_sample(W, 0xffffffffu, o.restart);
+    float4 ro, rd;
+    if (o.restart && init_path(W, slot, sid, &ro, &rd)) { o.ext = true; o.keep = true; }
+    int qs, qt, qe, qa;
+    queue_append<true>(W, next, false, o.trw, o.itw || o.ext, o.keep, &qs, &qt, &qe, &qa);
+    if (o.trw) {
+        float4 to, td;
+        trw_ray(W, slot, &to, &td);
+        push_ray4(W, qt, slot, WF_RAY_TRW, to, td);
+    }
+    if (o.itw) {
+        const float4 io = W.itw_o[slot], id = W.itw_d[slot];
+        push_ray4(W, qe, slot, WF_RAY_MIS, io, make_float4(id.x, id.y, id.z, kFMax));
+    } else if (o.ext) {
+        if (!o.restart) { ro = W.ray_o[slot]; rd = W.ray_d[slot]; }
+        push_ray4(W, qe, slot, WF_RAY_EXT, ro, rd);
+    }
+    if (o.keep) set_active(W, next, qa, slot);
 }
 
 __global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
@@ -1119,10 +1117,10 @@ __global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState 
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int slot = -1;
-    bool keep = false;
-    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; keep = shade_vol_path(W, slot, status, stats, counting); }
-    const int a = block_append(&W.ctr->n_active[cur ^ 1], keep);
-    if (keep) set_active(W, cur ^ 1, a, slot);
+    VolOut o;
+    o.trw = o.itw = o.ext = o.keep = o.restart = false;
+    if (i < n) { slot = sorted ? W.sorted[i] : W.active[cur][i]; shade_vol_path(&o, W, slot, status, stats, counting); }
+    vol_queues(W, slot, cur ^ 1, o);
 }
 
 /* the active paths of this iteration, one thread each over the sorted list
