@@ -146,12 +146,6 @@ DF void ray4(const Ray& r, float4* o, float4* d) {
     *d = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
 }
 
-DF void push_ray(const WfState& W, int q, int path, int kind, const Ray& r) {
-    if (!in_bounds(W, q, 3LL * W.slots)) return;
-    W.q_o[q] = make_float4(r.O.x, r.O.y, r.O.z, r.MinT);
-    W.q_d[q] = make_float4(r.D.x, r.D.y, r.D.z, r.MaxT);
-    W.q_meta[q] = (path << 10) | ((int)W.job[path] << 2) | kind;
-}
 DF int meta_path(int meta) { return meta >> 10; }
 DF int meta_job(int meta) { return (meta >> 2) & (WF_MAX_JOBS - 1); }
 DF int meta_kind(int meta) { return meta & 3; }
