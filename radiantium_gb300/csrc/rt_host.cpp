@@ -134,8 +134,6 @@ void ensure_events(Ctx* c, size_t n) {
     }
 }
 
-void set_err(Ctx* c, const std::string& m) { if (c) c->err = m; }
-
 template <class T>
 T* upload(Ctx* c, const std::vector<T>& v) {
     DevBuf b;
