@@ -291,8 +291,12 @@ int rt_render_device(void* ctx, const rt_render_params* params, float* d_out_rgb
  * GPU, a frame loop that cannot take cudaFree's device-wide synchronisation).
  * It always runs the megakernel renderer, whatever rt_set_renderer chose, out
  * of one static device array of RT_NOALLOC_SCRATCH_BYTES.  The first call on
- * a device sets that array up (the runtime loads its module and reserves it),
- * so make one call before any stream capture or allocation-free phase begins.
+ * a device sets that array up (looks up its device address; under lazy module
+ * loading, the CUDA 12.2+ default, this is also when the runtime loads its
+ * module and reserves the array - with CUDA_MODULE_LOADING=EAGER it is
+ * reserved when the context is created), so make one call before any stream
+ * capture or allocation-free phase begins.  Every call waits for its stream
+ * to drain before it returns (it reads the render's status word).
  * The film sums and one sample plane must fit:
  * 512 + 2 * 12 * width * height <= RT_NOALLOC_SCRATCH_BYTES (crop size; a
  * 1024 x 1024 crop fits), else RT_ERR_INVALID_ARG.  Counters are not

@@ -6,6 +6,7 @@
  */
 #include <atomic>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 #include <string>
 #include "or_scene.h"
@@ -393,6 +394,11 @@ static inline C3 RenderSample(const Scene& scene, const rt_render_params& P, int
     return color;
 }
 
+static int MaxThreads(int threads) {
+    if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
+    return threads > 0 ? threads : 1;
+}
+
 template <class F>
 static void ParallelFor(int64_t n, int threads, F fn) {
     if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
@@ -430,11 +436,23 @@ void or_scene_destroy(void* s) { delete (Scene*)s; }
 
 static inline Ray RayFrom(const rt_ray& r) { return Ray(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), r.min_t, r.max_t); }
 
-int or_trace_closest(void* sp, const rt_ray* rays, int64_t n, rt_hit* hits, int threads) {
+/* traversal counters of a ray batch, summed over the worker threads */
+static void SumTraceCounters(const std::vector<Counters>& counters, rt_stats* stats) {
+    if (!stats) return;
+    memset(stats, 0, sizeof(*stats));
+    for (const Counters& c : counters) {
+        stats->node_visits += c.node_visits; stats->prim_tests += c.prim_tests;
+        stats->instance_visits += c.instance_visits;
+    }
+}
+
+int or_trace_closest(void* sp, const rt_ray* rays, int64_t n, rt_hit* hits, int threads, rt_stats* stats) {
     const Scene* s = (const Scene*)sp;
     if (!s || n < 0) return RT_ERR_INVALID_ARG;
     std::atomic<int> overflow(0);
-    ParallelFor(n, threads, [&](int64_t i, int) {
+    std::vector<Counters> counters(MaxThreads(threads));
+    ParallelFor(n, threads, [&](int64_t i, int tid) {
+        tl_counters = stats ? &counters[tid] : nullptr;
         Intersection inct;
         tl_stack_overflow = false;
         bool hit = s->Aggregate->Intersect(RayFrom(rays[i]), &inct);
@@ -446,18 +464,24 @@ int or_trace_closest(void* sp, const rt_ray* rays, int64_t n, rt_hit* hits, int 
         } else {
             h.t = kFloatMax; h.u = 0; h.v = 0; h.prim = -1; h.sub = -1; h.flags = 0;
         }
+        tl_counters = nullptr;
     });
+    SumTraceCounters(counters, stats);
     return overflow ? RT_ERR_STACK : RT_OK;
 }
-int or_trace_any(void* sp, const rt_ray* rays, int64_t n, uint8_t* occ, int threads) {
+int or_trace_any(void* sp, const rt_ray* rays, int64_t n, uint8_t* occ, int threads, rt_stats* stats) {
     const Scene* s = (const Scene*)sp;
     if (!s || n < 0) return RT_ERR_INVALID_ARG;
     std::atomic<int> overflow(0);
-    ParallelFor(n, threads, [&](int64_t i, int) {
+    std::vector<Counters> counters(MaxThreads(threads));
+    ParallelFor(n, threads, [&](int64_t i, int tid) {
+        tl_counters = stats ? &counters[tid] : nullptr;
         tl_stack_overflow = false;
         occ[i] = s->Aggregate->IntersectP(RayFrom(rays[i])) ? 1 : 0;
         if (tl_stack_overflow) overflow = 1;
+        tl_counters = nullptr;
     });
+    SumTraceCounters(counters, stats);
     return overflow ? RT_ERR_STACK : RT_OK;
 }
 
@@ -661,6 +685,26 @@ int or_bvh(void* sp, int which, int64_t* node_count, int64_t* prim_count, float*
         idx[i] = nd.PrimitivesIndex; count[i] = nd.PrimitiveCount; axis[i] = nd.Axis;
     }
     for (size_t i = 0; prim_order && i < b->prims.size(); i++) prim_order[i] = b->prims[i]->id;
+    return RT_OK;
+}
+
+int or_scene_lights(void* sp, int64_t* count, int32_t* kind, int32_t* prim, float* le) {
+    const Scene* s = (const Scene*)sp;
+    if (!s || !count) return RT_ERR_INVALID_ARG;
+    *count = (int64_t)s->Lights.size();
+    if (!kind || !prim || !le) return RT_OK;
+    std::unordered_map<const Light*, int> owner;
+    for (const Primitive* p : s->Aggregate->prims)
+        if (const AreaLight* a = p->GetLight()) owner[a] = p->id;
+    for (size_t i = 0; i < s->Lights.size(); i++) {
+        const AreaLight* a = dynamic_cast<const AreaLight*>(s->Lights[i]);
+        kind[i] = a ? 0 : 1;
+        auto it = a ? owner.find(a) : owner.end();
+        prim[i] = it != owner.end() ? it->second : -1;
+        le[3 * i + 0] = a ? a->LightEmit.r : 0.0f;
+        le[3 * i + 1] = a ? a->LightEmit.g : 0.0f;
+        le[3 * i + 2] = a ? a->LightEmit.b : 0.0f;
+    }
     return RT_OK;
 }
 

@@ -16,9 +16,10 @@ extern "C" {
 void* or_scene_create(const rt_scene_desc* scene, char* err, int errlen);
 void or_scene_destroy(void* s);
 
-/* Scene.Intersect / Scene.Intersect(ray) over a batch (threads <= 0: all cores) */
-int or_trace_closest(void* s, const rt_ray* rays, int64_t n, rt_hit* hits, int threads);
-int or_trace_any(void* s, const rt_ray* rays, int64_t n, uint8_t* occluded, int threads);
+/* Scene.Intersect / Scene.Intersect(ray) over a batch (threads <= 0: all cores);
+ * stats (nullable) receives the summed node, primitive and instance visits */
+int or_trace_closest(void* s, const rt_ray* rays, int64_t n, rt_hit* hits, int threads, rt_stats* stats);
+int or_trace_any(void* s, const rt_ray* rays, int64_t n, uint8_t* occluded, int threads, rt_stats* stats);
 
 /* BlockBasedRenderer over the crop; out_rgb in ColorBuffer layout of the crop.
  * stats (nullable) receives the summed counters. */
@@ -48,6 +49,11 @@ int or_camera_rays(void* s, const float* screen_pos, int64_t n, rt_ray* out);
  * Call with NULL arrays to query sizes. */
 int or_bvh(void* s, int which, int64_t* node_count, int64_t* prim_count,
            float* bounds, int32_t* idx, int32_t* count, int32_t* axis, int32_t* prim_order);
+
+/* Scene.Lights in order: kind 0 = DiffuseAreaLight (prim = id of the
+ * aggregate primitive that carries it, le = its radiance), 1 = infinite light
+ * (prim -1, le 0).  Call with NULL arrays to query the count. */
+int or_scene_lights(void* s, int64_t* count, int32_t* kind, int32_t* prim, float* le);
 
 /* deterministic math and RNG known-answer hooks */
 int or_detmath(int fn, const float* a, const float* b, float* out, int64_t n);

@@ -35,8 +35,8 @@ def lib():
         L.or_scene_create.restype = vp
         L.or_scene_create.argtypes = [C.POINTER(N.SceneDescC), C.c_char_p, C.c_int]
         L.or_scene_destroy.argtypes = [vp]
-        L.or_trace_closest.argtypes = [vp, vp, C.c_int64, vp, C.c_int]
-        L.or_trace_any.argtypes = [vp, vp, C.c_int64, vp, C.c_int]
+        L.or_trace_closest.argtypes = [vp, vp, C.c_int64, vp, C.c_int, C.POINTER(N.Stats)]
+        L.or_trace_any.argtypes = [vp, vp, C.c_int64, vp, C.c_int, C.POINTER(N.Stats)]
         L.or_render.argtypes = [vp, C.POINTER(N.RenderParams), vp, C.c_int, C.POINTER(N.Stats)]
         L.or_render_samples.argtypes = [vp, C.POINTER(N.RenderParams), vp, C.c_int]
         L.or_render_particles.argtypes = [vp, C.POINTER(N.RenderParams), C.c_int64, C.c_int64, vp, C.c_int,
@@ -45,6 +45,7 @@ def lib():
                                          C.c_int]
         L.or_camera_rays.argtypes = [vp, vp, C.c_int64, vp]
         L.or_bvh.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp, vp, vp, vp, vp]
+        L.or_scene_lights.argtypes = [vp, C.POINTER(C.c_int64), vp, vp, vp]
         L.or_detmath.argtypes = [C.c_int, vp, vp, vp, C.c_int64]
         L.or_philox.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, vp]
         L.or_philox_raw.argtypes = [vp, vp, vp]
@@ -78,21 +79,27 @@ class OracleScene:
         except Exception:
             pass
 
-    def trace_closest(self, rays: np.ndarray, threads: int = 0) -> np.ndarray:
+    def trace_closest(self, rays: np.ndarray, threads: int = 0, stats: bool = False):
+        """Scene.Intersect per ray; with stats, also the summed traversal counters."""
         rays = np.ascontiguousarray(rays, dtype=N.ray_dtype())
         hits = np.zeros(rays.shape[0], dtype=N.hit_dtype())
-        rc = lib().or_trace_closest(self.h, _ptr(rays), rays.shape[0], _ptr(hits), threads)
+        st = N.Stats()
+        rc = lib().or_trace_closest(self.h, _ptr(rays), rays.shape[0], _ptr(hits), threads,
+                                    C.byref(st) if stats else None)
         if rc != 0:
             raise N.RTError(rc, "oracle trace_closest")
-        return hits
+        return (hits, st.as_dict()) if stats else hits
 
-    def trace_any(self, rays: np.ndarray, threads: int = 0) -> np.ndarray:
+    def trace_any(self, rays: np.ndarray, threads: int = 0, stats: bool = False):
+        """Scene.IsOccluded-style any hit per ray; with stats, also the summed traversal counters."""
         rays = np.ascontiguousarray(rays, dtype=N.ray_dtype())
         occ = np.zeros(rays.shape[0], dtype=np.uint8)
-        rc = lib().or_trace_any(self.h, _ptr(rays), rays.shape[0], _ptr(occ), threads)
+        st = N.Stats()
+        rc = lib().or_trace_any(self.h, _ptr(rays), rays.shape[0], _ptr(occ), threads,
+                                C.byref(st) if stats else None)
         if rc != 0:
             raise N.RTError(rc, "oracle trace_any")
-        return occ
+        return (occ, st.as_dict()) if stats else occ
 
     def render(self, settings, threads: int = 0, stats: bool = False):
         w = settings.width or (self.scene.camera.width - settings.x0)
@@ -157,6 +164,16 @@ class OracleScene:
         order = np.zeros(npr.value, dtype=np.int32)
         lib().or_bvh(self.h, which, C.byref(nn), C.byref(npr), _ptr(b), _ptr(idx), _ptr(cnt), _ptr(ax), _ptr(order))
         return {"bounds": b, "index": idx, "count": cnt, "axis": ax, "prim_order": order}
+
+    def lights(self) -> dict:
+        """Scene.Lights in order: kind (0 area, 1 infinite), carrying primitive id, radiance."""
+        n = C.c_int64()
+        lib().or_scene_lights(self.h, C.byref(n), None, None, None)
+        kind = np.zeros(n.value, dtype=np.int32)
+        prim = np.zeros(n.value, dtype=np.int32)
+        le = np.zeros((n.value, 3), dtype=np.float32)
+        lib().or_scene_lights(self.h, C.byref(n), _ptr(kind), _ptr(prim), _ptr(le))
+        return {"kind": kind, "prim": prim, "le": le}
 
 
 DETMATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan": 3, "atan2": 4, "acos": 5, "exp": 6, "log": 7}

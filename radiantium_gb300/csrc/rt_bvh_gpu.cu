@@ -446,24 +446,24 @@ cudaError_t rt_gpu_build_sah(const std::vector<rtb::Box>& bounds, int max_prims,
     int nodes_used = 1, nseg = 1;
     const int max_nodes = 2 * n;
     const int nbs = (n + 1023) / 1024 + 2;
-    GK(cudaMalloc(&d_box, (size_t)n * 6 * sizeof(float)));
+    GK(rt_dev_malloc((void**)&d_box, (size_t)n * 6 * sizeof(float)));
     GK(cudaMemcpyAsync(d_box, bounds.data(), (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice, s));
     D.box = d_box;
-    GK(cudaMalloc(&D.cent, (size_t)n * 3 * sizeof(float)));
-    GK(cudaMalloc(&D.perm, (size_t)n * sizeof(int)));
-    GK(cudaMalloc(&D.perm2, (size_t)n * sizeof(int)));
-    GK(cudaMalloc(&D.item_seg, (size_t)n * sizeof(int)));
-    GK(cudaMalloc(&D.fflag, (size_t)(n + 1) * sizeof(int)));
-    GK(cudaMalloc(&D.tflag, (size_t)(n + 1) * sizeof(int)));
-    GK(cudaMalloc(&D.fpos, (size_t)n * sizeof(int)));
-    GK(cudaMalloc(&D.tpos, (size_t)n * sizeof(int)));
-    GK(cudaMalloc(&D.bsum, (size_t)nbs * sizeof(int)));
-    GK(cudaMalloc(&D.seg, (size_t)n * sizeof(Seg)));
-    GK(cudaMalloc(&D.seg2, (size_t)n * sizeof(Seg)));
-    GK(cudaMalloc(&D.acc, (size_t)n * sizeof(SegAcc)));
-    GK(cudaMalloc(&D.plan, (size_t)n * sizeof(SegPlan)));
-    GK(cudaMalloc(&D.split, (size_t)(n + 1) * sizeof(int)));
-    GK(cudaMalloc(&D.nodes, (size_t)max_nodes * sizeof(GNode)));
+    GK(rt_dev_malloc((void**)&D.cent, (size_t)n * 3 * sizeof(float)));
+    GK(rt_dev_malloc((void**)&D.perm, (size_t)n * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.perm2, (size_t)n * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.item_seg, (size_t)n * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.fflag, (size_t)(n + 1) * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.tflag, (size_t)(n + 1) * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.fpos, (size_t)n * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.tpos, (size_t)n * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.bsum, (size_t)nbs * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.seg, (size_t)n * sizeof(Seg)));
+    GK(rt_dev_malloc((void**)&D.seg2, (size_t)n * sizeof(Seg)));
+    GK(rt_dev_malloc((void**)&D.acc, (size_t)n * sizeof(SegAcc)));
+    GK(rt_dev_malloc((void**)&D.plan, (size_t)n * sizeof(SegPlan)));
+    GK(rt_dev_malloc((void**)&D.split, (size_t)(n + 1) * sizeof(int)));
+    GK(rt_dev_malloc((void**)&D.nodes, (size_t)max_nodes * sizeof(GNode)));
     k_init<<<gridn(n, 256), 256, 0, s>>>(D);
     {
         const Seg root{0, n, 0, 0};

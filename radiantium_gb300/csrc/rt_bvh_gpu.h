@@ -8,6 +8,10 @@
 #include <vector>
 #include "rt_bvh.h"
 
+/* cudaMalloc that also counts the call in a process-wide tally (rt_host.cpp),
+ * so tests can show which entry points allocate device memory */
+cudaError_t rt_dev_malloc(void** p, size_t bytes);
+
 cudaError_t rt_gpu_build_sah(const std::vector<rtb::Box>& bounds, int max_prims, rtb::BuildResult* out, cudaStream_t s);
 
 #endif

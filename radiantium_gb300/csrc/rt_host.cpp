@@ -35,6 +35,13 @@
 #include <nvtx3/nvToolsExt.h>
 #include "rt_wavefront.h"
 
+static std::atomic<unsigned long long> g_device_allocs{0};
+
+cudaError_t rt_dev_malloc(void** p, size_t bytes) {
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
+    return cudaMalloc(p, bytes);
+}
+
 namespace {
 
 /* NVTX range over a scope: calls and wavefront phases show up named in
@@ -138,7 +145,7 @@ template <class T>
 T* upload(Ctx* c, const std::vector<T>& v) {
     DevBuf b;
     b.bytes = std::max<size_t>(sizeof(T), v.size() * sizeof(T));
-    CK(cudaMalloc(&b.p, b.bytes));
+    CK(rt_dev_malloc(&b.p, b.bytes));
     c->scene_bufs.push_back(b);
     if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
     return (T*)b.p;
@@ -158,7 +165,7 @@ void ensure(T** p, size_t* have, size_t need) {
     if (*have >= need && *p) return;
     if (*p) cudaFree(*p);
     *p = nullptr; *have = 0;
-    CK(cudaMalloc((void**)p, need));
+    CK(rt_dev_malloc((void**)p, need));
     *have = need;
 }
 
@@ -166,7 +173,7 @@ template <class T>
 T* wf_alloc(Ctx* c, size_t n) {
     DevBuf b;
     b.bytes = std::max<size_t>(sizeof(T), n * sizeof(T));
-    CK(cudaMalloc(&b.p, b.bytes));
+    CK(rt_dev_malloc(&b.p, b.bytes));
     c->wf_bufs.push_back(b);
     return (T*)b.p;
 }
@@ -205,9 +212,9 @@ void ensure_wf(Ctx* c, int slots) {
     W.itw_o = wf_alloc<float4>(c, n); W.itw_d = wf_alloc<float4>(c, n); W.itw_tr = wf_alloc<float4>(c, n);
     W.vol_li = wf_alloc<float4>(c, n);
     W.trw_hit = wf_alloc<float4>(c, n); W.trw_sub = wf_alloc<int32_t>(c, n);
-    if (!c->d_ctr) CK(cudaMalloc((void**)&c->d_ctr, sizeof(WfCounters)));
+    if (!c->d_ctr) CK(rt_dev_malloc((void**)&c->d_ctr, sizeof(WfCounters)));
     if (!c->h_ctr) CK(cudaMallocHost((void**)&c->h_ctr, sizeof(WfCounters)));
-    if (!c->d_jobs) CK(cudaMalloc((void**)&c->d_jobs, WF_MAX_JOBS * sizeof(WfJob)));
+    if (!c->d_jobs) CK(rt_dev_malloc((void**)&c->d_jobs, WF_MAX_JOBS * sizeof(WfJob)));
     if (!c->h_jobs) CK(cudaMallocHost((void**)&c->h_jobs, WF_MAX_JOBS * sizeof(WfJob)));
     W.ctr = c->d_ctr;
     W.jobs = c->d_jobs;
@@ -997,7 +1004,7 @@ void particle_splats(Ctx* c, const rt_render_params* p, int64_t first, int64_t c
         throw RtFail(RT_ERR_INVALID_ARG, "particle_splats: bad output");
     const size_t nb = (size_t)count * 4, pb = (size_t)count * max_per * 4, rb = pb * 3;
     char* buf = nullptr;
-    CK(cudaMalloc((void**)&buf, nb + pb + rb + 16));
+    CK(rt_dev_malloc((void**)&buf, nb + pb + rb + 16));
     struct Free { char* b; ~Free() { cudaFree(b); } } guard{buf};
     int32_t* dn = (int32_t*)buf;
     int32_t* dp = (int32_t*)(buf + nb);
@@ -1052,7 +1059,12 @@ void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t 
     c->cancel.store(0);
     uint64_t launches = 0, chunks = 0;
     for (int b = 0; b < P.spp; b += chunk) {
-        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        if (c->cancel.load()) {
+            /* the queued chunks still write the shared array: let them finish
+             * so the next call, from any context, starts on an idle array */
+            cudaStreamSynchronize(s);
+            throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        }
         P.chunk_begin = b;
         P.chunk_len = std::min(chunk, P.spp - b);
         CK(rt_launch_render(c->d_view, P, samples, status, stats, false, s));
@@ -1498,8 +1510,8 @@ int rt_create(int device, void** out_ctx) {
     c->device = device;
     int rc = run(c, [&]() {
         CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-        CK(cudaMalloc((void**)&c->status, 4));
-        CK(cudaMalloc((void**)&c->stats, 8 * sizeof(unsigned long long)));
+        CK(rt_dev_malloc((void**)&c->status, 4));
+        CK(rt_dev_malloc((void**)&c->stats, 8 * sizeof(unsigned long long)));
     });
     if (rc != RT_OK) { delete c; return rc; }
     *out_ctx = c;
@@ -1699,6 +1711,13 @@ int rt_debug_bvh_gpu(void* ctx, const float* boxes, int n, int max_prims, int64_
         }
     });
 }
+/* test hook (not part of radiantium.h): how many device allocations the
+ * library has made in this process, over every context */
+int rt_debug_device_allocations(unsigned long long* out) {
+    if (!out) return RT_ERR_INVALID_ARG;
+    *out = g_device_allocs.load(std::memory_order_relaxed);
+    return RT_OK;
+}
 /* test hook: primitive count from which upload_scene builds trees on the GPU */
 int rt_debug_set_gpu_build(void* ctx, int min_prims) {
     Ctx* c = (Ctx*)ctx;
@@ -1713,7 +1732,7 @@ int rt_debug_detmath(void* ctx, int fn, const float* a, const float* b, float* o
     Ctx* c = (Ctx*)ctx;
     return run(c, [&]() {
         float* d = nullptr;
-        CK(cudaMalloc((void**)&d, (size_t)n * 12 + 16));
+        CK(rt_dev_malloc((void**)&d, (size_t)n * 12 + 16));
         cudaError_t e = cudaSuccess;
         e = cudaMemcpyAsync(d, a, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d + n, b, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);

@@ -6,9 +6,13 @@
  * start-up, or a frame loop that cannot afford the device-wide
  * synchronisation cudaFree brings with it.  For them the megakernel render
  * (k_render + k_accumulate + k_finalize in rt_kernels.cu) runs out of this one
- * array.  It lives in its own translation unit, so its module - and the
- * RT_NOALLOC_SCRATCH_BYTES the runtime reserves for it - is loaded only by the
- * first lookup below, never by the other entry points.  The layout is set by
+ * array.  It lives in its own translation unit.  Under lazy module loading
+ * (CUDA_MODULE_LOADING=LAZY, the default of CUDA 12.2 and later) its module -
+ * and the RT_NOALLOC_SCRATCH_BYTES the runtime reserves for it - is loaded
+ * only by the first lookup below, never by the other entry points; with
+ * CUDA_MODULE_LOADING=EAGER every process that loads the library reserves the
+ * array when its context is created, whether it renders this way or not.
+ * The layout is set by
  * render_noalloc in rt_host.cpp: status word, counters, film sums, then one
  * chunk of per-sample radiance.
  */

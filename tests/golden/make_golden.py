@@ -77,6 +77,29 @@ def particle_cases():
             ("instanced", *procedural.instanced_spheres(48, 32, sphere_n=12, grid=4, env_w=64, env_h=32))]
 
 
+REFERENCE_SCENES = os.path.join(ROOT, "tests", "fixtures", "reference")
+
+
+def reference_scene_cases():
+    """(name, scene, settings) of the reference's own example scenes
+    (tests/fixtures/reference): a 32 x 32 crop at the film's centre, 8 spp, for
+    the path / vol_path scenes; the light-tracer scenes' settings for their
+    per-particle splats."""
+    from radiantium_gb300 import config
+    from tests.fixtures.reference.copy_reference_scenes import SCENES
+    cases = []
+    for rel in SCENES:
+        r = config.load_scene_file(os.path.join(REFERENCE_SCENES, rel))
+        cam, st = r.scene.camera, r.settings
+        name = rel.replace("/", "_").replace(".json", "")
+        if st.integrator != N.INTEGRATOR_PARTICLE:
+            st = st.replace(spp=8, seed=1, x0=cam.width // 2 - 16, y0=cam.height // 2 - 16, width=32, height=32)
+        else:
+            st = st.replace(seed=3)
+        cases.append((name, r.scene, st))
+    return cases
+
+
 def generate():
     out = {}
     rng = np.random.default_rng(2024)
@@ -121,6 +144,17 @@ def generate():
         out[f"particles_{name}"] = {"n": n, "pix": pix, "rgb": rgb.view(np.uint32),
                                     "film": film.astype(np.float32).view(np.uint32)}
         orc.close()
+    # the reference's example scenes
+    ref = {}
+    for name, scene, st in reference_scene_cases():
+        orc = oracle.OracleScene(scene)
+        if st.integrator == N.INTEGRATOR_PARTICLE:
+            n, pix, rgb = orc.particle_splats(st, 256, 12, first=77)
+            ref[name + "_n"], ref[name + "_pix"], ref[name + "_rgb"] = n, pix, rgb.view(np.uint32)
+        else:
+            ref[name + "_film"] = orc.render(st).astype(np.float32).view(np.uint32)
+        orc.close()
+    out["reference_scenes"] = ref
     return out
 
 

@@ -31,7 +31,7 @@ def _bits(a):
 @pytest.mark.parametrize("name", ["philox", "detmath", "hits_cornell", "hits_instanced", "bvh_cornell",
                                   "film_cornell_bxdf", "film_cornell_nee", "film_cornell_mis",
                                   "film_cornell_mis_all", "film_zoo_mis", "film_volume",
-                                  "particles_cornell", "particles_zoo", "particles_instanced"])
+                                  "particles_cornell", "particles_zoo", "particles_instanced", "reference_scenes"])
 def test_oracle_reproduces_golden(regenerated, name):
     want = _load(name)
     got = regenerated[name]

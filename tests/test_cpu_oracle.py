@@ -106,6 +106,25 @@ def test_bvh_matches_oracle_displaced_sphere(ensure_lib, n):
     _assert_same_tree(_lib_bvh(_tri_boxes(mesh)), O.OracleScene(s).bvh(-1))
 
 
+@pytest.mark.parametrize("name", ["C2", "C3", "C4"])
+def test_bvh_matches_oracle_benchmark_geometries(ensure_lib, name):
+    """The host builder at the benchmark sizes: the 199,692-triangle instanced
+    prototype, the 499,392-triangle vol_path scene and the largest batched
+    scene (1,572,528 triangles + ground + light) give the oracle's tree."""
+    if name == "C2":
+        s, _ = procedural.instanced_spheres(16, 16, env_w=8, env_h=4)
+        boxes, which = _tri_boxes(s.meshes[s.blas[0][0].ref]), 0
+    else:
+        s, _ = procedural.volume_sphere(16, 16) if name == "C3" else procedural.batch_scene(8)
+        boxes = np.concatenate([_tri_boxes(s.meshes[g.ref]) for g in s.groups if g.kind == N.GROUP_MESH])
+        which = -1
+    orc = O.OracleScene(s)
+    try:
+        _assert_same_tree(_lib_bvh(boxes), orc.bvh(which))
+    finally:
+        orc.close()
+
+
 def test_bvh_matches_oracle_cornell_and_prototype(ensure_lib):
     s, _ = procedural.cornell_box(16, 16)
     boxes = np.concatenate([_tri_boxes(m) for m in s.meshes])

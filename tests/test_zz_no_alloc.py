@@ -6,7 +6,11 @@ as rt_render_device, so the tolerance is zero: every float of the film must
 match.  Two calls in a row reuse the array with different crops, seeds and
 integrators, so state left over from the previous call would show.  The file
 name makes pytest collect it last; it also passes alone in a fresh process.
+A call after the first also leaves the device's free memory and the library's
+count of device allocations unchanged: it allocates nothing.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -18,6 +22,16 @@ from radiantium_gb300.device import Device
 pytestmark = pytest.mark.gpu
 
 TOLERANCE_ULP = 0   # bit-identical films
+
+
+def _device_allocations(dev):
+    """The library's process-wide count of device allocations (a test hook)."""
+    n = C.c_ulonglong()
+    f = dev.lib.rt_debug_device_allocations
+    f.argtypes = [C.POINTER(C.c_ulonglong)]
+    f.restype = C.c_int
+    assert f(C.byref(n)) == 0
+    return n.value
 
 
 def _film(fn, settings, w, h):
@@ -59,6 +73,25 @@ def test_noalloc_matches_render_device_on_consecutive_calls(scenes):
         _assert_same(got, want)
         again = _film(d.render_device_noalloc, st, w, h)
         _assert_same(again, want)
+
+
+def test_noalloc_second_call_allocates_nothing(scenes):
+    """The property the entry point exists for: once the scratch array is set
+    up, a call takes no device memory (cudaMemGetInfo) and makes no allocation."""
+    (d_cb, cb_st), _ = scenes
+    st = cb_st.replace(spp=5, seed=3, x0=4, y0=2, width=64, height=60)
+    out = torch.empty(64 * 60 * 3, dtype=torch.float32, device="cuda:0")
+    d_cb.render_device_noalloc(st, out.data_ptr())              # sets the scratch array up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    n0 = _device_allocations(d_cb)
+    for seed in (4, 5):
+        d_cb.render_device_noalloc(st.replace(seed=seed), out.data_ptr())
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert _device_allocations(d_cb) == n0
+    assert free1 == free0, (free0, free1)
+    assert torch.isfinite(out).all()
 
 
 def test_noalloc_rejects_crop_over_scratch(scenes):
