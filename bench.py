@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
     ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
     ap.add_argument("--no-relmse", action="store_true", help="skip the converged render for relMSE")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="instanced workload: skip the batch and adjoint sub-records after the headline timing")
     ap.add_argument("--autotune", choices=["on", "off"], default="off",
                     help="path workloads: pick the wavefront settings with rt_autotune on one step (untimed); "
                          "off by default: the defaults were as fast on C1-C3, and a 1-spp probe picked settings "
@@ -100,31 +102,66 @@ def workload_config(name, scene, st, spp_step):
     }
 
 
+CPU_GRID, CPU_TILE = 4, 16     # the CPU samples: a 4 x 4 grid of 16 x 16 tiles spread over the film
+
+
+def cpu_tiles(scene):
+    """Origins of the CPU sample's tiles: the centres of a 4 x 4 grid over the
+    film, so that background, edges and the dense middle are all in the sample."""
+    W, H = scene.camera.width, scene.camera.height
+    size = min(CPU_TILE, W, H)
+    tiles = []
+    for i in range(CPU_GRID):
+        for j in range(CPU_GRID):
+            x0 = min(W - size, max(0, int(round((i + 0.5) * W / CPU_GRID - size / 2))))
+            y0 = min(H - size, max(0, int(round((j + 0.5) * H / CPU_GRID - size / 2))))
+            tiles.append((x0, y0))
+    return size, tiles
+
+
+def oracle_tiles(orc, st, size, tiles, spp, begin, cores):
+    """Renders every tile at `spp` samples per pixel from sample index `begin`
+    on `cores` host threads; returns the samples rendered.  The work is cut into
+    (tile, sample range) items of one oracle thread each, taken dynamically, so
+    cheap and expensive tiles keep every core busy."""
+    from concurrent.futures import ThreadPoolExecutor
+    chunk = max(1, spp // 4)
+    items = [(x0, y0, b, min(chunk, spp - b)) for (x0, y0) in tiles for b in range(0, spp, chunk)]
+
+    def one(it):
+        x0, y0, b, n = it
+        orc.render(st.replace(spp=n, sample_begin=begin + b, x0=x0, y0=y0, width=size, height=size), threads=1)
+
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(one, items))
+    return len(tiles) * size * size * spp
+
+
+def tiles_desc(size, tiles, spp):
+    return (f"{len(tiles)} tiles of {size}x{size} pixels on a {CPU_GRID}x{CPU_GRID} grid over the film x {spp} spp "
+            f"({len(tiles) * size * size * spp} samples)")
+
+
 def cpu_baseline(scene, st, target_s, threads=0):
     """Times the CPU oracle (the reference path restated in C++) on a bounded
-    centre crop of the same workload, all host cores."""
+    sample of the same workload: 16 tiles spread over the film, all host cores."""
     from oracle.oracle import OracleScene
     cores = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     orc = OracleScene(scene)
     build_s = time.perf_counter() - t0
-    w = min(64, scene.camera.width)
-    h = min(64, scene.camera.height)
-    x0, y0 = (scene.camera.width - w) // 2, (scene.camera.height - h) // 2
-    cal = st.replace(spp=1, x0=x0, y0=y0, width=w, height=h)
+    size, tiles = cpu_tiles(scene)
     t0 = time.perf_counter()
-    orc.render(cal, threads=cores)
+    oracle_tiles(orc, st, size, tiles, 1, 0, cores)
     t1 = time.perf_counter() - t0
     spp = int(max(1, min(st.spp, target_s / max(t1, 1e-3))))
-    run = cal.replace(spp=spp)
     t0 = time.perf_counter()
-    orc.render(run, threads=cores)
+    samples = oracle_tiles(orc, st, size, tiles, spp, 1, cores)
     dt = time.perf_counter() - t0
-    samples = w * h * spp
     orc.close()
     return {"value": samples / dt, "unit": "samples/s", "cores": cores, "kind": "port",
-            "sample": f"centre {w}x{h} crop x {spp} spp of the same workload ({samples} samples, {dt:.1f} s; "
-                      f"oracle scene build {build_s:.1f} s not timed)"}
+            "sample": f"{tiles_desc(size, tiles, spp)} of the same workload ({dt:.1f} s; oracle scene build "
+                      f"{build_s:.1f} s not timed)"}
 
 
 class ClockSampler:
@@ -171,8 +208,10 @@ def measured_peak():
 
 
 def profiled_traffic(name, key="bytes_per_sample"):
-    """Per-sample (or per-particle) DRAM traffic of the traversal kernels from the
-    committed ncu summary (profiles/trace_<workload>_traffic.txt: one line `<key>=<x>`)."""
+    """A figure of the traversal kernels from the committed ncu summary
+    (profiles/trace_<workload>_traffic.txt: one line `<key>=<x>`): per-sample (or
+    per-particle) DRAM traffic by default, or the limiter figures of the
+    one-kernel capture."""
     p = os.path.join(ROOT, "profiles", f"trace_{name}_traffic.txt")
     if not os.path.exists(p):
         return None
@@ -190,33 +229,30 @@ def run_reference(args):
     from oracle.oracle import OracleScene
     cores = os.cpu_count() or 1
     orc = OracleScene(scene)
-    w = min(64, scene.camera.width)
-    h = min(64, scene.camera.height)
-    x0, y0 = (scene.camera.width - w) // 2, (scene.camera.height - h) // 2
-    cal = st.replace(spp=1, x0=x0, y0=y0, width=w, height=h)
+    size, tiles = cpu_tiles(scene)
     t0 = time.perf_counter()
-    orc.render(cal, threads=cores)
+    oracle_tiles(orc, st, size, tiles, 1, 0, cores)
     t1 = time.perf_counter() - t0
     # each step: a bounded sample sized so the whole run stays within a few minutes
     total_steps = args.steps + args.warmup
     spp = int(max(1, min(st.spp, (150.0 / total_steps) / max(t1, 1e-3))))
-    step = cal.replace(spp=spp)
     for i in range(args.warmup):
-        orc.render(step.replace(sample_begin=i * spp), threads=cores)
+        oracle_tiles(orc, st, size, tiles, spp, i * spp, cores)
     times = []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        orc.render(step.replace(sample_begin=(args.warmup + i) * spp), threads=cores)
+        samples = oracle_tiles(orc, st, size, tiles, spp, (args.warmup + i) * spp, cores)
         times.append(time.perf_counter() - t0)
-    samples = w * h * spp
+    orc.close()
     ms = 1000.0 * float(np.mean(times))
     value = samples / (ms / 1000.0)
-    sample_desc = f"centre {w}x{h} crop x {spp} spp per step ({samples} samples/step)"
+    sample_desc = tiles_desc(size, tiles, spp) + " per step"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": dict(workload_config(args.workload, scene, st, spp), step=sample_desc),
+        "config": workload_config(args.workload, scene, st, args.spp_per_step),
+        "run": {"step": sample_desc, "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
                          "sample": sample_desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
                                                  "(oracle/) runs on all host cores"},
@@ -388,6 +424,10 @@ def run_ours(args):
     achieved = alg_bytes_step / (kernel_ms / args.steps / 1000.0) / 1e9
     peak, peak_src = measured_peak()
     tps = profiled_traffic(args.workload) if uses_wavefront else None
+    # the limiter of the trace kernels, from the committed one-kernel capture
+    l2f = profiled_traffic(args.workload, "l2_throughput_frac") if uses_wavefront else None
+    lanes = profiled_traffic(args.workload, "threads_per_warp_instruction") if uses_wavefront else None
+    issue = profiled_traffic(args.workload, "issue_slots_busy_frac") if uses_wavefront else None
     traffic = None if tps is None else tps * samples_step / launches_per_step
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -397,20 +437,23 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": dict(workload_config(args.workload, scene, st, spp_step),
-                       parallelism=f"replicas x{world} (independent sample passes)",
-                       l2="256 MiB flush between timed steps (outside the CUDA events)",
-                       renderer=("wavefront (trace / shade kernels over compacted queues, path regeneration)"
-                                 + (", bounce loop as a CUDA graph" if graph_loop else "")
-                                 if uses_wavefront else "plain megakernel (one thread per camera sample)"),
-                       autotune=tuned),
+        "config": workload_config(args.workload, scene, st, spp_step),
+        "run": {"parallelism": f"replicas x{world} (independent sample passes)",
+                "l2": "256 MiB flush between timed steps (outside the CUDA events)",
+                "renderer": ("wavefront (trace / shade kernels over compacted queues, path regeneration)"
+                             + (", bounce loop as a CUDA graph" if graph_loop else "")
+                             if uses_wavefront else "plain megakernel (one thread per camera sample)"),
+                "autotune": tuned},
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_wf_trace_closest + k_wf_trace_shadow" if uses_wavefront else "k_render",
                      "alg_bytes_per_launch": alg_bytes_step / launches_per_step, "launch_ms": launch_ms,
                      "launches_per_step": launches_per_step,
-                     "kernel_ms_per_step": kernel_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps},
+                     "kernel_ms_per_step": kernel_ms / args.steps, "shade_ms_per_step": shade_ms / args.steps,
+                     "l2_frac": l2f, "lanes_per_instr": lanes, "issue_slots_busy": issue,
+                     "limiter_source": (f"profiles/trace_{args.workload}_traffic.txt (ncu --set full, one launch of "
+                                        "k_wf_trace_closest)") if l2f is not None else None},
         "plain_megakernel": plain,
         "relmse": relmse,
         "cpu_baseline": cpu,
@@ -420,12 +463,46 @@ def run_ours(args):
         "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
                                                    "prim_tests", "instance_visits", "invalid_samples")},
     }
+    dev.close()
+    del film, flush, frame
+    if args.workload == "instanced" and world == 1 and not args.no_subrecords:
+        line["batch"] = batch_subrecord(args, rank, world, local, dist)
+        line["adjoint"] = adjoint_subrecord(args, rank, world, local, dist)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    dev.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def batch_subrecord(args, rank, world, local, dist):
+    """The batched workload (32 scenes, one wavefront per step) for a few steps,
+    with the same steps scene by scene on the plain megakernel and on the
+    one-scene wavefront: the batched / plain ratio at equal relMSE (every
+    renderer gives the same films)."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.plain_steps, sub.renderer = 4, 3, 1, "auto"
+    sub.no_e2e, sub.no_cpu_baseline = True, True
+    b = batch_line(sub, rank, world, local, dist)
+    plain, seq = b["plain_megakernel"]["value"], b["sequential_wavefront"]["value"]
+    return {"value": b["value"], "unit": b["unit"], "steps": sub.steps, "warmup": sub.warmup,
+            "ms_per_step": b["ms_per_step"], "plain_megakernel": plain, "vs_plain_megakernel": b["value"] / plain,
+            "sequential_wavefront": seq, "vs_sequential_wavefront": b["value"] / seq,
+            "autotune": b["run"]["autotune"], "mrays_per_s": b["mrays_per_s"],
+            "roofline_frac": b["roofline"]["frac"], "config": b["config"],
+            "note": "bench.py --workload batch: 32 scenes as one wavefront (rt_render_batch_device) vs the same "
+                    "passes scene by scene (plain megakernel, one-scene wavefront); identical films"}
+
+
+def adjoint_subrecord(args, rank, world, local, dist):
+    """The adjoint workload for a few steps, with its finite-difference checks per
+    parameter group (albedo texels, patch alphas)."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.no_cpu_baseline = 4, 3, True
+    a = adjoint_line(sub, rank, world, local, dist)
+    return dict(a["adjoint"], steps=sub.steps, warmup=sub.warmup, config=a["config"],
+                note="bench.py --workload adjoint: forward + dL/dI + backward per step; fd_check: central finite "
+                     "differences with common random numbers per parameter group")
 
 
 BATCH_STEPS_PER_FRAME = 16
@@ -491,7 +568,8 @@ def run_batch_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-        "config": dict(batch_config(scenes, batch_step_settings(scenes, 0)), step=desc),
+        "config": batch_config(scenes, batch_step_settings(scenes, 0)),
+        "run": {"step": desc, "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
                          "sample": desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
                                           "(oracle/) runs on all host cores"},
@@ -503,21 +581,37 @@ def run_batch_reference(args):
     return 0
 
 
+def ranks():
+    """(rank, world, local rank, torch.distributed or None); joins the NCCL group under torchrun."""
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return rank, world, local, dist
+
+
 def run_batch(args):
+    rank, world, local, dist = ranks()
+    line = batch_line(args, rank, world, local, dist)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def batch_line(args, rank, world, local, dist):
     """The batched workload: 32 scenes rendered as one wavefront per step."""
     import torch
     from radiantium_gb300 import native as N
     from radiantium_gb300 import procedural
     from radiantium_gb300.device import Device
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     scenes = procedural.batch_scenes()
     t0 = time.perf_counter()
     devs = []
@@ -646,12 +740,12 @@ def run_batch(args):
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-        "config": dict(batch_config(scenes, batch_step_settings(scenes, 0)),
-                       parallelism=f"replicas x{world} (independent sample passes)",
-                       l2="256 MiB flush between timed steps (outside the CUDA events)",
-                       renderer="batched wavefront, bounce loop as a CUDA graph while-loop" if graph
-                       else "batched wavefront, bounce loop driven from the host",
-                       autotune=tuned),
+        "config": batch_config(scenes, batch_step_settings(scenes, 0)),
+        "run": {"parallelism": f"replicas x{world} (independent sample passes)",
+                "l2": "256 MiB flush between timed steps (outside the CUDA events)",
+                "renderer": "batched wavefront, bounce loop as a CUDA graph while-loop" if graph
+                else "batched wavefront, bounce loop driven from the host",
+                "autotune": tuned},
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,
@@ -668,14 +762,10 @@ def run_batch(args):
         "counts_per_step": {k: counts[k] for k in ("samples", "rays_closest", "rays_shadow", "node_visits",
                                                    "prim_tests", "instance_visits", "invalid_samples")},
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     for d in devs:
         d.close()
     host.close()
-    if dist:
-        dist.destroy_process_group()
-    return 0
+    return line
 
 
 def adjoint_setup(d, prm, rng_seed=0):
@@ -695,19 +785,21 @@ def adjoint_setup(d, prm, rng_seed=0):
 
 
 def run_adjoint(args):
+    rank, world, local, dist = ranks()
+    line = adjoint_line(args, rank, world, local, dist)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def adjoint_line(args, rank, world, local, dist):
     """The adjoint workload: one step = forward film + L2-loss gradient + backward
     pass to every albedo texel and every patch alpha."""
     import torch
     from radiantium_gb300 import procedural
     from radiantium_gb300.device import Device
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     scene, st, prm = procedural.adjoint_patches()
     d = Device(local)
     d.upload(scene)
@@ -783,12 +875,29 @@ def run_adjoint(args):
             fds.append((lp - lm) / 0.02)
         set_params(alb0, alpha0)
         fd_r = float(np.mean(fds))
+        # material by material: the 4 largest |dL/dalpha| (steps of 5 % of that alpha), and one random
+        # direction over all alphas (2 % steps); 4 seeds x 4096 spp each
+        per = []
+        dirs = [(f"material {int(m)}", np.eye(alpha0.size)[m] * alpha0[m], 0.05) for m in np.argsort(-np.abs(gal))[:4]]
+        dirs.append(("random", np.random.default_rng(5).standard_normal(alpha0.size) * alpha0, 0.02))
+        for name, v, eps in dirs:
+            fdk = []
+            for k in range(4):
+                stx = st.replace(spp=4096, seed=200 + k)
+                set_params(alb0, alpha0 + eps * v); lp = lin(stx)
+                set_params(alb0, alpha0 - eps * v); lm = lin(stx)
+                fdk.append((lp - lm) / (2 * eps))
+            set_params(alb0, alpha0)
+            fdm, adm = float(np.mean(fdk)), float((gal.astype(np.float64) * v).sum())
+            per.append({"direction": name, "fd": fdm, "fd_stderr": float(np.std(fdk, ddof=1) / 2.0),
+                        "adjoint": adm, "rel_err": abs(fdm - adm) / abs(fdm)})
         check = {"albedo": {"fd": fd_a, "adjoint": ad_a, "rel_err": abs(fd_a - ad_a) / abs(fd_a),
                             "how": "random normal direction over all texels, eps 1e-3, common random numbers, 64 spp"},
                  "alpha": {"fd": fd_r, "fd_stderr": float(np.std(fds, ddof=1) / math.sqrt(len(fds))), "adjoint": ad_r,
                            "rel_err": abs(fd_r - ad_r) / abs(fd_r),
                            "how": "direction sign(grad) x alpha, eps 1 %, mean of 8 seeds x 4096 spp (common random "
                                   "numbers) vs adjoint at 16384 spp"},
+                 "alpha_per_direction": per,
                  "loss": "linearised L2: sum(w * I), w = 2 (I_1024spp - target)"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -803,9 +912,9 @@ def run_adjoint(args):
                                "patches sharing a 512x512 albedo texture, Gaussian-lobe env; path MIS; L2 loss "
                                "against a film of perturbed parameters",
                    "film": [W, H], "spp": st.spp, "max_depth": st.max_depth, "parameters": int(n_params),
-                   "step": "forward render + dL/dI + backward (gradient w.r.t. all parameters)",
-                   "parallelism": f"replicas x{world}", "l2": "inputs resident; no flush (forward and backward "
-                   "re-read the scene)"},
+                   "step": "forward render + dL/dI + backward (gradient w.r.t. all parameters)"},
+        "run": {"parallelism": f"replicas x{world}",
+                "l2": "inputs resident; no flush (forward and backward re-read the scene)"},
         "adjoint": {"grads_per_s": world / s_step, "params_per_s": n_params * world / s_step,
                     "backward_ms": bwd_ms / args.steps, "forward_ms": 1000.0 * fwd_s,
                     "fd_params_per_s": 1.0 / (2.0 * fwd_s),
@@ -819,12 +928,8 @@ def run_adjoint(args):
         "gpu_launches": int(fwd_launches * args.steps + bwd_launches),
         "clocks": clk,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     d.close()
-    if dist:
-        dist.destroy_process_group()
-    return 0
+    return line
 
 
 def particle_workload():
@@ -887,7 +992,8 @@ def run_particle_reference(args):
         "impl": "reference", "metric": "particles/s (adjoint_particle light tracer)", "value": value,
         "unit": "particles/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded procedural scene)", "config": dict(particle_config(scene, st, n), step=desc),
+        "data": "synthetic (seeded procedural scene)", "config": particle_config(scene, st, args.particles_per_step),
+        "run": {"step": desc, "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
                          "sample": desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
                                           "(oracle/) runs on all host cores"},
@@ -1025,12 +1131,13 @@ def run_particles(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded procedural scene)",
-        "config": dict(particle_config(scene, st, per), parallelism=f"replicas x{world} (disjoint particle ranges)",
-                       l2="256 MiB flush between timed steps (outside the CUDA events)",
-                       renderer=("wavefront (trace / shade kernels over compacted queues, particle regeneration)"
-                                 + (", bounce loop as a CUDA graph" if mode != N.RENDERER_WAVEFRONT else "")
-                                 if wavefront else "megakernel k_particles (one thread per particle)")
-                       + " + k_particle_finish"),
+        "config": particle_config(scene, st, per),
+        "run": {"parallelism": f"replicas x{world} (disjoint particle ranges)",
+                "l2": "256 MiB flush between timed steps (outside the CUDA events)",
+                "renderer": ("wavefront (trace / shade kernels over compacted queues, particle regeneration)"
+                             + (", bounce loop as a CUDA graph" if mode != N.RENDERER_WAVEFRONT else "")
+                             if wavefront else "megakernel k_particles (one thread per particle)")
+                + " + k_particle_finish"},
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,

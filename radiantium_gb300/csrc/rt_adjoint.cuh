@@ -94,7 +94,31 @@ DF bool UsesAlbedo(const RtSceneView* S, int albedo_tex, int mi) {
     return (m.type == RT_MAT_DIFFUSE || m.type == RT_MAT_ROUGH_PLASTIC) && m.tex_r == albedo_tex;
 }
 
-/* credits g (rgb, per unit R) to the texel footprint of TexSample at uv */
+/* adds v to the three floats at o with one atomic per distinct address per
+ * warp: the lanes that reach this call together are grouped by address
+ * (__match_any_sync), each group sums its values by shuffles in lane order
+ * and its lowest lane adds the sums.  Lanes with o == nullptr only take part
+ * in the exchange. */
+DF void WarpAggregatedAdd3(float* o, C3 v) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, (unsigned long long)o);
+    const int lane = (int)(threadIdx.x & 31);
+    float r = 0.0f, g = 0.0f, b = 0.0f;
+    for (unsigned m = peers; m; m &= m - 1) {
+        const int src = __ffs(m) - 1;
+        r += __shfl_sync(peers, v.r, src);
+        g += __shfl_sync(peers, v.g, src);
+        b += __shfl_sync(peers, v.b, src);
+    }
+    if (o && lane == __ffs(peers) - 1) {
+        if (r != 0.0f) atomicAdd(o + 0, r);
+        if (g != 0.0f) atomicAdd(o + 1, g);
+        if (b != 0.0f) atomicAdd(o + 2, b);
+    }
+}
+
+/* credits g (rgb, per unit R) to the texel footprint of TexSample at uv; the
+ * lanes of a warp that credit the same texel share one atomic per channel */
 DF void ScatterAlbedo(const RtSceneView* S, int albedo_tex, float* grad_albedo, V2 uv, C3 g) {
     const RtTexture t = S->textures[albedo_tex];
     const float u = Wrapper(uv.x, t.wrap), v = Wrapper(uv.y, t.wrap);
@@ -111,11 +135,9 @@ DF void ScatterAlbedo(const RtSceneView* S, int albedo_tex, float* grad_albedo, 
         ws[0] = (1 - du) * (1 - dv); ws[1] = du * (1 - dv); ws[2] = (1 - du) * dv; ws[3] = du * dv;
     }
     for (int q = 0; q < 4; q++) {
-        if (ws[q] == 0.0f) continue;
-        float* o = grad_albedo + ((int64_t)xs[q] * t.height + ys[q]) * 3;
-        if (g.r != 0.0f) atomicAdd(o + 0, g.r * ws[q]);
-        if (g.g != 0.0f) atomicAdd(o + 1, g.g * ws[q]);
-        if (g.b != 0.0f) atomicAdd(o + 2, g.b * ws[q]);
+        const bool any = ws[q] != 0.0f && (g.r != 0.0f || g.g != 0.0f || g.b != 0.0f);
+        float* o = any ? grad_albedo + ((int64_t)xs[q] * t.height + ys[q]) * 3 : nullptr;
+        WarpAggregatedAdd3(o, c3(g.r * ws[q], g.g * ws[q], g.b * ws[q]));
     }
 }
 

@@ -129,7 +129,8 @@ def displaced_sphere(n: int, seed: int, amplitude: float = 0.06, frequency: floa
     cube = np.concatenate(pos)
     idx = np.concatenate(idx).astype(np.int32)
     dirs = cube / np.sqrt((cube * cube).sum(1, keepdims=True))
-    r = 1.0 + amplitude * value_noise(dirs * frequency, seed)
+    # amplitude 0 (the displaced box's base sphere) leaves r = 1 exactly: skip the noise
+    r = 1.0 + amplitude * value_noise(dirs * frequency, seed) if amplitude != 0.0 else np.ones(dirs.shape[0])
     p = (dirs * r[:, None]).astype(np.float32)
     idx = _orient_outward(p, idx, np.zeros(3))
     return Mesh(p, idx)
