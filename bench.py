@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
+    ap.add_argument("--traversal", choices=["exact", "wide"], default="exact",
+                    help="exact: the reference's tree and order (bit-exact films); wide: the opt-in fast traversal")
     ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
     ap.add_argument("--no-relmse", action="store_true", help="skip the converged render for relMSE")
     ap.add_argument("--no-subrecords", action="store_true",
@@ -102,12 +104,14 @@ def workload_config(name, scene, st, spp_step):
     }
 
 
-CPU_GRID, CPU_TILE = 4, 16     # the CPU samples: a 4 x 4 grid of 16 x 16 tiles spread over the film
+CPU_GRID, CPU_TILE = 8, 8      # the CPU samples: an 8 x 8 grid of 8 x 8 tiles spread over the film
 
 
 def cpu_tiles(scene):
-    """Origins of the CPU sample's tiles: the centres of a 4 x 4 grid over the
-    film, so that background, edges and the dense middle are all in the sample."""
+    """Origins of the CPU sample's tiles: the centres of an 8 x 8 grid over the
+    film, so that background, edges and the dense middle are all in the sample
+    (the reference renders a pixel's samples one after another, and so does
+    each tile)."""
     W, H = scene.camera.width, scene.camera.height
     size = min(CPU_TILE, W, H)
     tiles = []
@@ -137,14 +141,30 @@ def oracle_tiles(orc, st, size, tiles, spp, begin, cores):
     return len(tiles) * size * size * spp
 
 
+def tiles_work(orc, st, size, tiles, cores):
+    """Node visits per sample of the tiles at 1 spp (untimed): how the sample's
+    traversal work compares with the whole film's."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(t):
+        _, c = orc.render(st.replace(spp=1, x0=t[0], y0=t[1], width=size, height=size), threads=1, stats=True)
+        return c["node_visits"], c["samples"]
+
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        r = list(ex.map(one, tiles))
+    return sum(a for a, _ in r) / max(1, sum(b for _, b in r))
+
+
 def tiles_desc(size, tiles, spp):
     return (f"{len(tiles)} tiles of {size}x{size} pixels on a {CPU_GRID}x{CPU_GRID} grid over the film x {spp} spp "
             f"({len(tiles) * size * size * spp} samples)")
 
 
-def cpu_baseline(scene, st, target_s, threads=0):
+def cpu_baseline(scene, st, target_s, threads=0, frame_nodes_per_sample=None):
     """Times the CPU oracle (the reference path restated in C++) on a bounded
-    sample of the same workload: 16 tiles spread over the film, all host cores."""
+    sample of the same workload: 64 tiles spread over the film, all host cores.
+    frame_nodes_per_sample: the whole film's traversal work per sample (from the
+    GPU's counting pass), reported beside the sample's own."""
     from oracle.oracle import OracleScene
     cores = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
@@ -158,10 +178,12 @@ def cpu_baseline(scene, st, target_s, threads=0):
     t0 = time.perf_counter()
     samples = oracle_tiles(orc, st, size, tiles, spp, 1, cores)
     dt = time.perf_counter() - t0
+    work = tiles_work(orc, st, size, tiles, cores)
     orc.close()
     return {"value": samples / dt, "unit": "samples/s", "cores": cores, "kind": "port",
             "sample": f"{tiles_desc(size, tiles, spp)} of the same workload ({dt:.1f} s; oracle scene build "
-                      f"{build_s:.1f} s not timed)"}
+                      f"{build_s:.1f} s not timed)",
+            "sample_nodes_per_sample": work, "frame_nodes_per_sample": frame_nodes_per_sample}
 
 
 class ClockSampler:
@@ -243,6 +265,7 @@ def run_reference(args):
         t0 = time.perf_counter()
         samples = oracle_tiles(orc, st, size, tiles, spp, (args.warmup + i) * spp, cores)
         times.append(time.perf_counter() - t0)
+    work = tiles_work(orc, st, size, tiles, cores)
     orc.close()
     ms = 1000.0 * float(np.mean(times))
     value = samples / (ms / 1000.0)
@@ -255,7 +278,8 @@ def run_reference(args):
         "run": {"step": sample_desc, "parallelism": f"{cores} host threads"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
                          "sample": sample_desc + "; the C# reference cannot run here (no .NET), its C++ restatement "
-                                                 "(oracle/) runs on all host cores"},
+                                                 "(oracle/) runs on all host cores",
+                         "sample_nodes_per_sample": work},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -284,6 +308,7 @@ def run_ours(args):
     mode = {"auto": N.RENDERER_AUTO, "megakernel": N.RENDERER_MEGAKERNEL, "wavefront": N.RENDERER_WAVEFRONT,
             "graph": N.RENDERER_WAVEFRONT_GRAPH}[args.renderer]
     dev.set_renderer(mode)
+    traversal = N.TRAVERSAL_WIDE if args.traversal == "wide" else N.TRAVERSAL_EXACT
     uses_wavefront = mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) or (
         mode == N.RENDERER_AUTO and st.strategy == N.STRATEGY_UNIFORM)
     upload_s = time.perf_counter() - t0
@@ -312,6 +337,7 @@ def run_ours(args):
     counts = dev.stats()
     dev.set_counting(False)
 
+    dev.set_traversal(traversal)            # the counting pass above ran the exact traversal
     for i in range(args.warmup):
         dev.render_device(st.replace(spp=spp_step, sample_begin=base + i * spp_step), film.data_ptr(), stream)
     torch.cuda.synchronize()
@@ -431,7 +457,8 @@ def run_ours(args):
     traffic = None if tps is None else tps * samples_step / launches_per_step
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(scene, st, args.cpu_seconds)
+        cpu = cpu_baseline(scene, st, args.cpu_seconds,
+                           frame_nodes_per_sample=counts["node_visits"] / max(1, counts["samples"]))
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
@@ -443,7 +470,10 @@ def run_ours(args):
                 "renderer": ("wavefront (trace / shade kernels over compacted queues, path regeneration)"
                              + (", bounce loop as a CUDA graph" if graph_loop else "")
                              if uses_wavefront else "plain megakernel (one thread per camera sample)"),
-                "autotune": tuned},
+                "autotune": tuned,
+                "traversal": ("exact (the reference's tree and visit order)" if traversal == N.TRAVERSAL_EXACT
+                              else "wide (opt-in fast traversal; the counting pass and algorithmic bytes use "
+                                   "the exact one)")},
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,

@@ -360,6 +360,25 @@ int rt_set_counting(void* ctx, int enabled);
 #define RT_RENDERER_WAVEFRONT_GRAPH 3
 int rt_set_renderer(void* ctx, int mode);
 
+/* ---- traversal mode (no counterpart in the reference) ------------------------
+ * RT_TRAVERSAL_EXACT (default): the reference's binary tree, visited in the
+ * order Bvh.Intersect visits it (Accelerators/Bvh.cs:126-232); hits, films
+ * and traversal counters equal the reference's restatement bit for bit.
+ * RT_TRAVERSAL_WIDE: an opt-in fast traversal for the wavefront renderers,
+ * batches and the ray-batch calls (the megakernel always runs the exact one):
+ * the same trees collapsed 8-wide with quantised child boxes read as six
+ * 16-byte loads per node, children visited near to far.  It finds the same
+ * closest primitive except where two candidates have exactly the same t
+ * (flagged RT_HIT_TIE by either traversal) or where the reference's own slab
+ * test misses a box at rounding scale; node-visit counters count wide nodes.
+ * A scene whose wide trees could overflow the 64-entry stack (or whose binary
+ * trees are deeper than 65 levels) renders with the exact traversal;
+ * rt_get_traversal reports what the next call will use. */
+#define RT_TRAVERSAL_EXACT 0
+#define RT_TRAVERSAL_WIDE 1
+int rt_set_traversal(void* ctx, int mode);
+int rt_get_traversal(void* ctx, int* effective);
+
 /* One render of a batch: the context holding its uploaded scene (may be the
  * batch context itself), its parameters and its host output film (crop,
  * ColorBuffer layout, width * height * 3 floats). */

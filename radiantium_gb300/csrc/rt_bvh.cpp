@@ -6,6 +6,8 @@
 #include "rt_bvh.h"
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <future>
 #include <limits.h>
 #include <utility>
@@ -193,6 +195,93 @@ BuildResult build_sah(const std::vector<Box>& prim_bounds, int max_prims, int th
     r.max_depth = b.build(r.nodes, 0, n, 0);
     r.order.resize(n);
     for (int i = 0; i < n; i++) r.order[i] = items[i].id;
+    return r;
+}
+
+/* ---- the wide tree of the fast traversal -------------------------------------------------- */
+
+/* The quantisation grid of one axis of a node box [mn, mx]: scale 2^k with k
+ * large enough that 253 steps cover the extent and that one step is at least
+ * 2^-20 of the coordinates' magnitude (so the one-step padding outweighs the
+ * rounding of the traversal's plane distances), origin one step below mn
+ * (rounded down).  Children are quantised outwards with one more step of
+ * padding; k grows until every child fits in [0, 255]. */
+static void quantise_axis(double mn, double mx, const std::vector<std::pair<double, double>>& kids, float* p,
+                          uint8_t* e, uint8_t* qlo, uint8_t* qhi) {
+    const double ext = mx - mn;
+    const double mag = std::max(std::max(std::fabs(mn), std::fabs(mx)), 1e-30);
+    int k = std::max(ext > 0 ? (int)std::ceil(std::log2(ext / 253.0)) : -126, (int)std::floor(std::log2(mag)) - 20);
+    for (k = std::max(k, -126); k <= 127; k++) {
+        const double s = std::ldexp(1.0, k);
+        float pf = (float)(mn - s);
+        if ((double)pf > mn - s) pf = std::nextafter(pf, -INFINITY);
+        bool ok = std::isfinite(pf);
+        int lo[8] = {0}, hi[8] = {0};
+        for (size_t c = 0; ok && c < kids.size(); c++) {
+            lo[c] = (int)std::floor((kids[c].first - (double)pf) / s) - 1;
+            hi[c] = (int)std::ceil((kids[c].second - (double)pf) / s) + 1;
+            ok = lo[c] >= 0 && hi[c] <= 255;
+        }
+        if (!ok) continue;
+        *p = pf;
+        *e = (uint8_t)(k + 127);
+        for (size_t c = 0; c < 8; c++) {
+            qlo[c] = c < kids.size() ? (uint8_t)lo[c] : 255;    /* empty slots: lo > hi, never hit */
+            qhi[c] = c < kids.size() ? (uint8_t)hi[c] : 0;
+        }
+        return;
+    }
+    *p = (float)mn; *e = 254;                                     /* unreachable for finite boxes */
+    for (int c = 0; c < 8; c++) { qlo[c] = 0; qhi[c] = 255; }
+}
+
+WideResult build_wide(const BuildResult& br) {
+    WideResult r;
+    const std::vector<FlatNode>& fn = br.nodes;
+    if (fn.empty() || fn[0].count != 0) return r;
+    struct Work { int bnode, wnode, push; };
+    std::vector<Work> work{{0, 0, 0}};
+    r.nodes.emplace_back();
+    while (!work.empty()) {
+        const Work w = work.back();
+        work.pop_back();
+        std::vector<int> kids{w.bnode + 1, fn[w.bnode].second};
+        while (kids.size() < 8) {
+            int best = -1;
+            float best_a = -1.0f;
+            for (size_t i = 0; i < kids.size(); i++) {
+                if (fn[kids[i]].count != 0) continue;
+                const float a = surface_area(fn[kids[i]].bounds);
+                if (a > best_a) { best_a = a; best = (int)i; }
+            }
+            if (best < 0) break;
+            const int b = kids[best];
+            kids[best] = b + 1;
+            kids.insert(kids.begin() + best + 1, fn[b].second);
+        }
+        WideNode& n = r.nodes[w.wnode];
+        std::memset(&n, 0, sizeof(n));
+        n.nchild = (uint8_t)kids.size();
+        const Box& nb = fn[w.bnode].bounds;
+        for (int a = 0; a < 3; a++) {
+            std::vector<std::pair<double, double>> iv;
+            for (int k : kids) iv.emplace_back((double)fn[k].bounds.mn[a], (double)fn[k].bounds.mx[a]);
+            quantise_axis((double)nb.mn[a], (double)nb.mx[a], iv, &n.p[a], &n.e[a], n.qlo[a], n.qhi[a]);
+        }
+        const int push = w.push + (int)kids.size() - 1;
+        r.max_push = std::max(r.max_push, w.push);
+        for (size_t i = 0; i < 8; i++) {
+            n.child[i] = i < kids.size() ? kids[i] : -1;
+            n.wchild[i] = -1;
+        }
+        for (size_t i = 0; i < kids.size(); i++) {
+            if (fn[kids[i]].count != 0) continue;
+            const int wi = (int)r.nodes.size();
+            r.nodes[w.wnode].wchild[i] = wi;     /* r.nodes may reallocate below: index, not the reference */
+            r.nodes.emplace_back();
+            work.push_back({kids[i], wi, push});
+        }
+    }
     return r;
 }
 

@@ -375,7 +375,9 @@ struct Best {
     V3 pw;           /* for instance candidates: world-space point */
 };
 
+#ifndef RT_TRAVERSAL_CAP
 #define RT_TRAVERSAL_CAP (1u << 26)   /* loop steps of one two-level traversal */
+#endif
 #ifndef RT_DESCEND
 /* interior nodes one traversal step may visit in shallow trees (Cornell box / light tracer,
  * M samples / particles per s: 415 / 223 at 2, 421 / 229 at 3, 426 / 227 at 4, 418 / 224 at 5) */
@@ -400,7 +402,9 @@ DF bool PrimHit(const RtSceneView* S, uint32_t kind, uint32_t ref, float4 s0, fl
 }
 
 /* Root box of tree `bvh`: RT_NO_NODE if the tree is empty or the box is
- * missed, else the root's reference (counts one node visit if non-empty). */
+ * missed, else the root's reference (counts one node visit if non-empty);
+ * kWide: the root of the tree's wide form. */
+template <bool kWide = false>
 DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
     const RtBvh h = S->bvhs[bvh];
     if (h.root_ref == RT_NO_NODE) return RT_NO_NODE;
@@ -409,7 +413,7 @@ DF int RootRef(const RtSceneView* S, int bvh, const Ray& r, TravStats* st) {
     if (!SlabA(h.root_min[0], h.root_min[1], h.root_min[2], h.root_max[0], h.root_max[1], h.root_max[2], r, &tmin) ||
         !(tmin < r.MaxT))
         return RT_NO_NODE;
-    return h.root_ref;
+    return kWide ? h.wide_root : h.root_ref;
 }
 
 /* Traversal stack storage: a thread-local array, or (SplitStack) the first
@@ -461,6 +465,93 @@ DF int VisitNode(const RtSceneView* S, int node, const Ray& r, Stk stack, int* s
     return (nearA && nearT < r.MaxT) ? nearRef : RT_NO_NODE;
 }
 
+/* two candidate distances within 4 ulp of each other: the fast traversal
+ * reports these as ties too (its conservative boxes can meet a candidate
+ * the reference's rounding-scale box test culled) */
+DF bool NearTie(float a, float b) {
+    const int d = __float_as_int(a) - __float_as_int(b);
+    return a >= 0.0f && b >= 0.0f && d >= -4 && d <= 4;
+}
+
+/* ---- the opt-in fast traversal: 8-wide nodes with quantised child boxes ----------------------
+ * One node holds up to eight children of the reference's tree (rtb::build_wide)
+ * with boxes quantised outwards on a per-node grid, read with six 16-byte
+ * loads.  The plane distances t = q * (s / d) + (p - o) / d are one fused
+ * multiply-add each - the only place the fast mode contracts - and every
+ * interval is widened by 2^-20 of its ends, so a child box is never missed
+ * where its exact box is hit: the fast traversal visits a superset of the
+ * boxes the reference's slab test accepts and finds every primitive hit the
+ * reference finds.  Hit children are ordered near to far by a sorting network
+ * over 32-bit keys (entry distance with its low three bits replaced by the
+ * child's index, which rounds the distance down); the nearest is descended
+ * into and the others are pushed far-first with the rounded-down distance,
+ * which PopNext checks against MaxT.  Primitive tests, instance entry and
+ * exit and the closest-hit rule are the exact traversal's; only the order in
+ * which equal-t candidates are met can differ.  Such ties are flagged
+ * RT_HIT_TIE as in the exact traversal, and so are candidates within 4 ulp
+ * of the best one (coplanar surfaces a ulp apart, of which the reference's
+ * box test culls the second at rounding scale). */
+/* byte k of `word` as a float: the byte placed in the mantissa of 2^23, minus 2^23 (exact) */
+DF float wq(uint32_t word, int k) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7650u | (uint32_t)k)) - 8388608.0f;
+}
+DF void ucas(uint32_t& a, uint32_t& b) { const uint32_t lo = umin(a, b), hi = umax(a, b); a = lo; b = hi; }
+
+template <class Stk>
+DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, int* sp) {
+    const float4* np = S->wnodes + RT_WIDE_F4 * (int64_t)node;
+    const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
+    const int4 ra = __ldg(reinterpret_cast<const int4*>(np + 4)), rb = __ldg(reinterpret_cast<const int4*>(np + 5));
+    const uint32_t meta = __float_as_uint(w0.w);
+    const float ax = __uint_as_float((meta & 0xffu) << 23) * r.InvD.x;
+    const float ay = __uint_as_float(((meta >> 8) & 0xffu) << 23) * r.InvD.y;
+    const float az = __uint_as_float(((meta >> 16) & 0xffu) << 23) * r.InvD.z;
+    const float bx = (w0.x - r.O.x) * r.InvD.x, by = (w0.y - r.O.y) * r.InvD.y, bz = (w0.z - r.O.z) * r.InvD.z;
+    /* near and far planes per axis by the direction's sign: words of children 0-3 and 4-7 */
+    const bool fx = r.InvD.x < 0, fy = r.InvD.y < 0, fz = r.InvD.z < 0;
+    const uint32_t nx0 = __float_as_uint(fx ? w1.z : w1.x), nx1 = __float_as_uint(fx ? w1.w : w1.y);
+    const uint32_t gx0 = __float_as_uint(fx ? w1.x : w1.z), gx1 = __float_as_uint(fx ? w1.y : w1.w);
+    const uint32_t ny0 = __float_as_uint(fy ? w2.z : w2.x), ny1 = __float_as_uint(fy ? w2.w : w2.y);
+    const uint32_t gy0 = __float_as_uint(fy ? w2.x : w2.z), gy1 = __float_as_uint(fy ? w2.y : w2.w);
+    const uint32_t nz0 = __float_as_uint(fz ? w3.z : w3.x), nz1 = __float_as_uint(fz ? w3.w : w3.y);
+    const uint32_t gz0 = __float_as_uint(fz ? w3.x : w3.z), gz1 = __float_as_uint(fz ? w3.y : w3.w);
+    const float kWiden = 9.5367431640625e-07f;   /* 2^-20 */
+    uint32_t key[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int b = k & 3;
+        const float tx0 = __fmaf_rn(wq(k < 4 ? nx0 : nx1, b), ax, bx), tx1 = __fmaf_rn(wq(k < 4 ? gx0 : gx1, b), ax, bx);
+        const float ty0 = __fmaf_rn(wq(k < 4 ? ny0 : ny1, b), ay, by), ty1 = __fmaf_rn(wq(k < 4 ? gy0 : gy1, b), ay, by);
+        const float tz0 = __fmaf_rn(wq(k < 4 ? nz0 : nz1, b), az, bz), tz1 = __fmaf_rn(wq(k < 4 ? gz0 : gz1, b), az, bz);
+        float tlo = fmaxf(fmaxf(tx0, ty0), tz0), thi = fminf(fminf(tx1, ty1), tz1);
+        tlo = __fmaf_rn(-fabsf(tlo), kWiden, tlo);
+        thi = __fmaf_rn(fabsf(thi), kWiden, thi);
+        const bool hit = k < (int)(meta >> 24) && tlo <= thi && thi >= 0.0f && tlo <= r.MaxT;
+        const float te = tlo > 0.0f ? tlo : 0.0f;
+        key[k] = hit ? ((__float_as_uint(te) & ~7u) | (uint32_t)k) : 0xffffffffu;
+    }
+    /* Batcher's odd-even merge sort of eight keys (19 compare-exchanges) */
+    ucas(key[0], key[1]); ucas(key[2], key[3]); ucas(key[4], key[5]); ucas(key[6], key[7]);
+    ucas(key[0], key[2]); ucas(key[1], key[3]); ucas(key[4], key[6]); ucas(key[5], key[7]);
+    ucas(key[1], key[2]); ucas(key[5], key[6]);
+    ucas(key[0], key[4]); ucas(key[1], key[5]); ucas(key[2], key[6]); ucas(key[3], key[7]);
+    ucas(key[2], key[4]); ucas(key[3], key[5]);
+    ucas(key[1], key[2]); ucas(key[3], key[4]); ucas(key[5], key[6]);
+    if (key[0] == 0xffffffffu) return RT_NO_NODE;
+#pragma unroll
+    for (int j = 7; j >= 1; j--) {
+        if (key[j] != 0xffffffffu) {
+            const uint32_t c = key[j] & 7u;
+            const int4 q = (c & 4u) ? rb : ra;
+            const int ref = (c & 2u) ? ((c & 1u) ? q.w : q.z) : ((c & 1u) ? q.y : q.x);
+            stk_put(stack, (*sp)++, make_int2(ref, (int)(key[j] & ~7u)));
+        }
+    }
+    const uint32_t c = key[0] & 7u;
+    const int4 q = (c & 4u) ? rb : ra;
+    return (c & 2u) ? ((c & 1u) ? q.w : q.z) : ((c & 1u) ? q.y : q.x);
+}
+
 /* Pops until an entry passes the MaxT check (Bvh.cs:205-229 / 153-169). */
 template <class Stk>
 DF int PopNext(Stk stack, int* sp, int base, float maxT, TravStats* st) {
@@ -506,6 +597,7 @@ struct TravClosest {
 };
 
 /* Returns true when the traversal is already over (empty scene or root box missed). */
+template <bool kWide = false>
 DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravStats* st) {
     Best& b = T.best;
     b.t = kFMax; b.flags = 0; b.slot = -1; b.sub = -1; b.u = 0; b.v = 0; b.pw = v3s(0);
@@ -514,20 +606,21 @@ DF bool ClosestBegin(const RtSceneView* S, const Ray& ray, TravClosest& T, TravS
     T.base = 0; T.sp = 0; T.leafLeft = 0; T.leafSlot = 0; T.topSlot = 0; T.topLeft = 0; T.inst = 0;
     T.pt = kFMax; T.pu = 0; T.pv = 0; T.pslot = -1; T.pflags = 0;
     T.guard = 0;
-    T.cur = RootRef(S, 0, ray, st);
+    T.cur = RootRef<kWide>(S, 0, ray, st);
     if (T.cur == RT_NO_NODE) return true;
     EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
     return false;
 }
 
-/* One step; true when the traversal has finished. */
-template <class Stk, int kDescend = RT_DESCEND>
+/* One step; true when the traversal has finished.  kWide: the fast traversal's
+ * wide nodes (a visit may push up to seven entries). */
+template <class Stk, int kDescend = RT_DESCEND, bool kWide = false>
 DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* status, TravStats* st) {
-    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_TRAV); return true; }
     if (T.cur != RT_NO_NODE) {
         /* up to kDescend interior nodes (with the pops that follow them) per step */
         for (int k = 0; k < kDescend && T.cur >= 0; k++) {
-            if (T.sp - T.base == RT_STACK_SIZE) {
+            if (kWide ? T.sp - T.base > RT_STACK_SIZE - 8 : T.sp - T.base == RT_STACK_SIZE) {
                 atomicOr(status, RT_STATUS_STACK);
                 if (!T.inProto) return true;
                 T.sp = T.base;                  /* the prototype's traversal stops here */
@@ -535,7 +628,7 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
                 return false;
             }
             if (st) st->nodes++;
-            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            T.cur = kWide ? VisitWideNode(S, T.cur, T.r, stack, &T.sp) : VisitNode(S, T.cur, T.r, stack, &T.sp, st);
             if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         }
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
@@ -555,10 +648,12 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
             if (!PrimHit(S, kind, ref, s0, s1, s2, T.r, &t, &u, &v)) {
             } else if (T.inProto) {
                 T.pany = true;
+                if (kWide && NearTie(t, T.pt)) T.pflags |= RT_HIT_TIE;
                 if (t < T.pt) { T.pt = t; T.pu = u; T.pv = v; T.pslot = slot; T.r.MaxT = t; }
                 else if (t == T.pt) T.pflags |= RT_HIT_TIE;
             } else {
                 T.any = true;
+                if (kWide && NearTie(t, T.best.t)) T.best.flags |= RT_HIT_TIE;
                 if (t < T.best.t) {
                     T.best.t = t; T.best.u = u; T.best.v = v; T.best.slot = slot; T.best.sub = -1; T.best.pw = v3s(0);
                     T.r.MaxT = t;
@@ -589,7 +684,7 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
         T.pt = kFMax; T.pu = 0; T.pv = 0; T.pslot = -1; T.pflags = 0; T.pany = false;
         T.inProto = true;
         T.base = T.sp;
-        T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        T.cur = RootRef<kWide>(S, 1 + __ldg(&I.blas), T.r, st);
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
@@ -618,6 +713,7 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
         const float t = Distance(T.wO, pw);
         T.any = true;
         T.best.flags |= T.pflags;
+        if (kWide && NearTie(t, T.best.t)) T.best.flags |= RT_HIT_TIE;
         if (t < T.best.t) {
             T.best.t = t; T.best.u = T.pu; T.best.v = T.pv; T.best.slot = T.topSlot - 1; T.best.sub = T.pslot; T.best.pw = pw;
             T.wMaxT = t;
@@ -637,10 +733,11 @@ DF bool ClosestStep(const RtSceneView* S, TravClosest& T, Stk stack, uint32_t* s
 }
 
 /* The whole closest-hit traversal of one ray; ray.MaxT ends at the closest hit. */
+template <bool kWide = false>
 DF bool SceneClosest(const RtSceneView* S, Ray& ray, Best* best, int2* stack, uint32_t* status, TravStats* st) {
     TravClosest T;
-    if (!ClosestBegin(S, ray, T, st))
-        while (!ClosestStep(S, T, stack, status, st)) {}
+    if (!ClosestBegin<kWide>(S, ray, T, st))
+        while (!ClosestStep<int2*, RT_DESCEND, kWide>(S, T, stack, status, st)) {}
     *best = T.best;
     ray.MaxT = T.inProto ? T.wMaxT : T.r.MaxT;
     return T.any;
@@ -657,24 +754,25 @@ struct TravAny {
     uint32_t guard;
 };
 
+template <bool kWide = false>
 DF bool AnyBegin(const RtSceneView* S, const Ray& ray, TravAny& T, TravStats* st) {
     T.r = ray; T.wO = ray.O; T.wD = ray.D; T.wMaxT = ray.MaxT;
     T.inProto = false; T.hit = false;
     T.base = 0; T.sp = 0; T.leafLeft = 0; T.leafSlot = 0; T.topSlot = 0; T.topLeft = 0;
     T.guard = 0;
-    T.cur = RootRef(S, 0, ray, st);
+    T.cur = RootRef<kWide>(S, 0, ray, st);
     if (T.cur == RT_NO_NODE) return true;
     EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
     return false;
 }
 
 /* One step; true when the traversal has finished (T.hit holds the answer). */
-template <class Stk, int kDescend = RT_DESCEND>
+template <class Stk, int kDescend = RT_DESCEND, bool kWide = false>
 DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, TravStats* st) {
-    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_ITER); return true; }
+    if (++T.guard > RT_TRAVERSAL_CAP) { atomicOr(status, RT_STATUS_TRAV); return true; }
     if (T.cur != RT_NO_NODE) {
         for (int k = 0; k < kDescend && T.cur >= 0; k++) {
-            if (T.sp - T.base == RT_STACK_SIZE) {
+            if (kWide ? T.sp - T.base > RT_STACK_SIZE - 8 : T.sp - T.base == RT_STACK_SIZE) {
                 atomicOr(status, RT_STATUS_STACK);
                 if (!T.inProto) return true;
                 T.sp = T.base;
@@ -682,7 +780,7 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, T
                 return false;
             }
             if (st) st->nodes++;
-            T.cur = VisitNode(S, T.cur, T.r, stack, &T.sp, st);
+            T.cur = kWide ? VisitWideNode(S, T.cur, T.r, stack, &T.sp) : VisitNode(S, T.cur, T.r, stack, &T.sp, st);
             if (T.cur == RT_NO_NODE) T.cur = PopNext(stack, &T.sp, T.base, T.r.MaxT, st);
         }
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
@@ -719,7 +817,7 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, T
         T.r = XfRay(T.r, w2m);
         T.inProto = true;
         T.base = T.sp;
-        T.cur = RootRef(S, 1 + __ldg(&I.blas), T.r, st);
+        T.cur = RootRef<kWide>(S, 1 + __ldg(&I.blas), T.r, st);
         EnterLeaf(S, &T.cur, &T.leafSlot, &T.leafLeft);
         return false;
     }
@@ -736,10 +834,11 @@ DF bool AnyStep(const RtSceneView* S, TravAny& T, Stk stack, uint32_t* status, T
     return false;
 }
 
+template <bool kWide = false>
 DF bool SceneAny(const RtSceneView* S, const Ray& ray, int2* stack, uint32_t* status, TravStats* st) {
     TravAny T;
-    if (!AnyBegin(S, ray, T, st))
-        while (!AnyStep(S, T, stack, status, st)) {}
+    if (!AnyBegin<kWide>(S, ray, T, st))
+        while (!AnyStep<int2*, RT_DESCEND, kWide>(S, T, stack, status, st)) {}
     return T.hit;
 }
 

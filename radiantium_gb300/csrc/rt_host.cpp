@@ -108,6 +108,8 @@ struct Ctx {
     int64_t sample_budget = 1 << 24;          /* samples per launch (sample buffer = 12 B each) */
     std::vector<cudaEvent_t> events;           /* per-launch timing of the path-tracing kernel */
     int renderer = RT_RENDERER_AUTO;
+    int traversal = RT_TRAVERSAL_EXACT;        /* rt_set_traversal */
+    int wf_iter_cap = WF_ITER_CAP;             /* bounce iterations of one wavefront round (test hook) */
     /* wavefront path state */
     WfState wf{};
     std::vector<DevBuf> wf_bufs;
@@ -308,6 +310,38 @@ rtb::BuildResult build_tree(Ctx* c, const std::vector<rtb::Box>& boxes, int maxp
     return rtb::build_sah(boxes, maxp, threads);
 }
 
+/* the wide form of a tree (rtb::build_wide) for the fast traversal; leaf refs
+ * are the binary tree's (first slot, count in that slot).  Returns the most
+ * stack entries a wide traversal of the tree can hold below a node. */
+int emit_wide(const rtb::BuildResult& br, int slot_base, std::vector<float4>& wnodes, RtBvh* hdr) {
+    const std::vector<rtb::FlatNode>& fn = br.nodes;
+    if (fn.empty()) { hdr->wide_root = INT_MIN; return 0; }
+    if (fn[0].count != 0) { hdr->wide_root = hdr->root_ref; return 0; }
+    const rtb::WideResult w = rtb::build_wide(br);
+    const int base = (int)(wnodes.size() / RT_WIDE_F4);
+    hdr->wide_root = base;
+    for (const rtb::WideNode& n : w.nodes) {
+        uint32_t meta = (uint32_t)n.e[0] | ((uint32_t)n.e[1] << 8) | ((uint32_t)n.e[2] << 16) | ((uint32_t)n.nchild << 24);
+        float4 f[RT_WIDE_F4];
+        f[0] = make_float4(n.p[0], n.p[1], n.p[2], 0.0f);
+        std::memcpy(&f[0].w, &meta, 4);
+        for (int a = 0; a < 3; a++) {
+            std::memcpy(&f[1 + a].x, n.qlo[a], 8);
+            std::memcpy(&f[1 + a].z, n.qhi[a], 8);
+        }
+        int32_t ref[8];
+        for (int k = 0; k < 8; k++) {
+            if (k >= n.nchild) ref[k] = INT_MIN;
+            else if (n.wchild[k] >= 0) ref[k] = base + n.wchild[k];
+            else ref[k] = ~(slot_base + fn[n.child[k]].second);
+        }
+        std::memcpy(&f[4], ref, 16);
+        std::memcpy(&f[5], ref + 4, 16);
+        for (int q = 0; q < RT_WIDE_F4; q++) wnodes.push_back(f[q]);
+    }
+    return w.max_push;
+}
+
 void emit_bvh(const rtb::BuildResult& br, const std::vector<std::array<float4, 3>>& recs, std::vector<float4>& nodes,
               std::vector<float4>& slots, RtBvh* hdr) {
     const int slot_base = (int)(slots.size() / 3);
@@ -444,7 +478,8 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
             throw RtFail(RT_ERR_INVALID_ARG, "scene: material " + std::to_string(i) + " is missing a texture or has an unknown type");
     }
 
-    std::vector<float4> nodes, slots;
+    std::vector<float4> nodes, slots, wnodes;
+    int wide_push = 0;
     std::vector<RtBvh> bvhs(1 + d->blas_count);
     /* instanced prototypes: ShapeWrapperPrimitive per shape (RendererBuilder.cs:895-921) */
     std::vector<rtb::Box> blas_root(d->blas_count);
@@ -472,7 +507,9 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
         }
         rtb::BuildResult br = build_tree(c, boxes, maxp, threads);
         tallest = std::max(tallest, br.max_depth);
+        const int blas_slots = (int)(slots.size() / 3);
         emit_bvh(br, recs, nodes, slots, &bvhs[1 + b]);
+        wide_push = std::max(wide_push, emit_wide(br, blas_slots, wnodes, &bvhs[1 + b]));
         if (!br.nodes.empty()) blas_root[b] = br.nodes[0].bounds;
         else blas_root[b] = rtb::empty_box();
     }
@@ -557,7 +594,9 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     if (prims.empty()) throw RtFail(RT_ERR_INVALID_ARG, "scene: no primitives");
     rtb::BuildResult top = build_tree(c, boxes, maxp, threads);
     tallest = std::max(tallest, top.max_depth);
+    const int top_slots = (int)(slots.size() / 3);
     emit_bvh(top, recs, nodes, slots, &bvhs[0]);
+    wide_push = std::max(wide_push, emit_wide(top, top_slots, wnodes, &bvhs[0]));
 
     /* textures */
     std::vector<RtTexture> texs(d->texture_count);
@@ -672,6 +711,10 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.global_medium = d->global_medium < 0 ? -1 : d->global_medium;
     v.deep_trees = tallest > RT_STACK_SIZE + 1 ? 1 : 0;
     c->tallest = tallest;
+    if (wnodes.empty()) wnodes.push_back(make_float4(0, 0, 0, 0));
+    v.wnodes = upload(c, wnodes);
+    /* a wide visit pushes at most 7 entries on top of what is below it */
+    v.wide_ok = (!v.deep_trees && wide_push + 7 <= RT_STACK_SIZE) ? 1 : 0;
     RtCamera& cam = v.camera;
     cam.width = d->camera.width; cam.height = d->camera.height;
     cam.near_z = d->camera.near_z; cam.far_z = d->camera.far_z;
@@ -701,14 +744,22 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     c->width = cam.width; c->height = cam.height;
 }
 
+/* the call's error for a device status word (rt_types.h RT_STATUS_*) */
+void throw_status(uint32_t st) {
+    if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
+    if (st & RT_STATUS_TRAV) throw RtFail(RT_ERR_ITER_CAP, "a BVH traversal reached its step cap (RT_TRAVERSAL_CAP)");
+    if (st & RT_STATUS_WALK) throw RtFail(RT_ERR_ITER_CAP, "a null-boundary walk reached its segment cap (RT_WALK_CAP)");
+    if (st & RT_STATUS_WFITER) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached (WF_ITER_CAP)");
+    if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a path reached its bounce cap (RT_LOOP_CAP)");
+    if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
+    if (st & RT_STATUS_BOUNDS) throw RtFail(RT_ERR_BOUNDS, "a device index left its buffer (debug-bounds build)");
+}
+
 void check_status(Ctx* c) {
     uint32_t st = 0;
     CK(cudaMemcpyAsync(&st, c->status, 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
-    if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
-    if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
-    if (st & RT_STATUS_BOUNDS) throw RtFail(RT_ERR_BOUNDS, "a device index left its buffer (debug-bounds build)");
+    throw_status(st);
 }
 
 void read_stats(Ctx* c) {
@@ -819,7 +870,8 @@ RtParams particle_params(Ctx* c, const rt_render_params* p, int64_t first, int64
     return P;
 }
 
-void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true, bool deep = false);
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle = false, bool sort = true, bool deep = false,
+                     bool wide = false);
 
 /* What a wavefront run shades, and how its kernels are chosen. */
 struct WfMode {
@@ -827,6 +879,7 @@ struct WfMode {
     bool particle = false;   /* light-tracer start / shade kernels */
     bool sort = true;        /* regroup the active list by shade key before shading */
     bool deep = false;       /* trace kernels with the shared-memory stack (trees of 16+ levels) */
+    bool wide = false;       /* the opt-in fast traversal over the wide nodes */
 };
 /* CUDA-event times and launch counts of a run, summed over its rounds */
 struct WfTotals {
@@ -848,7 +901,7 @@ void wf_round(Ctx* c, const WfState& W, cudaStream_t s, bool use_graph, const Wf
     CK(rt_wf_start(W, s, m.particle));
     t->launches += 2;
     if (use_graph && pass == WF_PASS_RENDER) {
-        ensure_wf_graph(c, W, m.vol, m.particle, m.sort, m.deep);
+        ensure_wf_graph(c, W, m.vol, m.particle, m.sort, m.deep, m.wide);
         CK(cudaEventRecord(c->events[0], s));
         CK(cudaGraphLaunch(c->wf_exec, s));
         CK(cudaEventRecord(c->events[1], s));
@@ -866,10 +919,10 @@ void wf_round(Ctx* c, const WfState& W, cudaStream_t s, bool use_graph, const Wf
     CK(cudaStreamSynchronize(s));
     while (c->h_ctr->n_active[c->h_ctr->iter & 1] > 0 || c->h_ctr->n_shadow > 0) {
         if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
-        if (c->h_ctr->iter >= WF_ITER_CAP) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached");
+        if (c->h_ctr->iter >= W.iter_cap) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached (WF_ITER_CAP)");
         NvtxRange nvtx_iter("rt.wavefront_iteration");
         CK(cudaEventRecord(c->events[0], s));
-        CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, m.deep));
+        CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, m.deep, m.wide));
         CK(cudaEventRecord(c->events[1], s));
         CK(cudaEventRecord(c->events[2], s));
         CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false, s,
@@ -908,10 +961,12 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
     W.slots = slots;
     W.shadow_base = 2 * slots;
     W.refill = c->wf_refill;
+    W.iter_cap = c->wf_iter_cap;
     WfMode m;
     m.particle = true;
     m.sort = c->mat_types > 1;
     m.deep = c->tallest >= RT_DEEP_TREE;
+    m.wide = c->traversal == RT_TRAVERSAL_WIDE && c->view.wide_ok;
     WfTotals t;
     for (int64_t done = 0; done < count;) {
         if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
@@ -1081,10 +1136,7 @@ void render_noalloc(Ctx* c, const rt_render_params* p, float* dst, cudaStream_t 
     c->last.samples = (uint64_t)npix * P.spp;
     c->last.render_launches = chunks;
     c->last.kernel_launches = launches + 1;
-    if (st & RT_STATUS_STACK) throw RtFail(RT_ERR_STACK, "BVH traversal stack (64 entries) overflowed");
-    if (st & RT_STATUS_ITER) throw RtFail(RT_ERR_ITER_CAP, "a device loop reached its iteration cap");
-    if (st & RT_STATUS_BADREF) throw RtFail(RT_ERR_INVALID_ARG, "an instanced prototype contains an instance");
-    if (st & RT_STATUS_BOUNDS) throw RtFail(RT_ERR_BOUNDS, "a device index left its buffer (debug-bounds build)");
+    throw_status(st);
 }
 
 /* one render of a wavefront run: scene, parameters (full spp), film sums */
@@ -1094,14 +1146,16 @@ struct WfJobIn {
     float* film;
     int mat_types;         /* distinct material types of the job's scene */
     int tallest;           /* levels of its tallest tree */
+    bool wide_ok;          /* its wide trees fit the fast traversal's stack */
 };
 
 /* The bounce loop as a graph: a while node whose body is one iteration
  * (trace, phase, sort, shade, tail); the tail kernel clears the loop's
  * condition when no path is left.  Rebuilt when the path state moves or the
  * counting mode changes. */
-void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sort, bool deep) {
-    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)W.slots << 10) ^ ((uint64_t)deep << 9) ^
+void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sort, bool deep, bool wide) {
+    const uint64_t key = (c->wf_generation << 32) ^ ((uint64_t)wide << 63) ^ ((uint64_t)W.slots << 10) ^ ((uint64_t)deep << 9) ^
+                         ((uint64_t)(uint32_t)W.iter_cap * 0x9E3779B97F4A7C15ull) ^
                          ((uint64_t)sort << 8) ^ ((uint64_t)particle << 7) ^ ((uint64_t)W.refill << 2) ^
                          ((uint64_t)vol << 1) ^ (c->counting ? 1u : 0u);
     if (c->wf_exec && c->wf_graph_key == key) return;
@@ -1120,7 +1174,7 @@ void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sor
     cudaGraph_t body = np.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     uint64_t launches = 0;
-    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream, deep);
+    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream, deep, wide);
     cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches,
                                  WF_PASS_RENDER, nullptr, vol, particle, sort);
     cudaGraph_t captured = nullptr;
@@ -1154,6 +1208,8 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
     mode.vol = vol;
     mode.sort = vol || adj || jobs.size() > 1 || jobs[0].mat_types > 1;
     for (const WfJobIn& J : jobs) mode.deep = mode.deep || J.tallest >= RT_DEEP_TREE;
+    mode.wide = c->traversal == RT_TRAVERSAL_WIDE;
+    for (const WfJobIn& J : jobs) mode.wide = mode.wide && J.wide_ok;
     ensure_events(c, 4);
     WfTotals tot;
     while (true) {
@@ -1193,6 +1249,7 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         W.slots = slots;
         W.shadow_base = 2 * slots;
         W.refill = c->wf_refill;
+        W.iter_cap = c->wf_iter_cap;
         /* one pass over the round's samples: start every slot, bounce until no path is left */
         auto run_pass = [&](int pass) {
             wf_round(c, W, s, use_graph, mode, pass, adj, total, (int)act.size(), &tot);
@@ -1222,6 +1279,7 @@ void render_wavefront(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t 
     jobs[0].film = c->film;
     jobs[0].mat_types = c->mat_types;
     jobs[0].tallest = c->tallest;
+    jobs[0].wide_ok = c->view.wide_ok != 0;
     /* AUTO drives vol_path's loop as a graph: its boundary walks make ~100 short iterations per
      * round, where the host loop's per-iteration synchronisation costs 9 % (C3) */
     const bool vol = P.integrator == RT_INTEGRATOR_VOL_PATH;
@@ -1261,6 +1319,7 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
         jobs[i].P = P;
         jobs[i].mat_types = sc->mat_types;
         jobs[i].tallest = sc->tallest;
+        jobs[i].wide_ok = sc->view.wide_ok != 0;
         film_off[i] = film_floats;
         film_floats += (int64_t)P.w * P.h * 3;
     }
@@ -1363,6 +1422,7 @@ void adjoint_backward(Ctx* c, const rt_render_params* p, const rt_adjoint_desc* 
         jobs[0].film = nullptr;
         jobs[0].mat_types = c->mat_types;
         jobs[0].tallest = c->tallest;
+        jobs[0].wide_ok = c->view.wide_ok != 0;
         CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
         wavefront_run(c, jobs, s, false, &A);
         launches += c->last.kernel_launches;
@@ -1461,7 +1521,8 @@ void trace(Ctx* c, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ, bo
         char* ob = base + (((size_t)n * sizeof(rt_ray) + 255) & ~(size_t)255);
         if (hits) dh = (rt_hit*)ob; else dob = (uint8_t*)ob;
     }
-    CK(rt_launch_trace(c->d_view, dr, n, dh, dob, c->status, c->stats, c->counting, s));
+    CK(rt_launch_trace(c->d_view, dr, n, dh, dob, c->status, c->stats, c->counting, s,
+                       c->traversal == RT_TRAVERSAL_WIDE && c->view.wide_ok));
     if (host && n > 0) {
         if (hits) CK(cudaMemcpyAsync(hits, dh, (size_t)n * sizeof(rt_hit), cudaMemcpyDeviceToHost, s));
         else CK(cudaMemcpyAsync(occ, dob, (size_t)n, cudaMemcpyDeviceToHost, s));
@@ -1644,6 +1705,19 @@ int rt_cancel(void* ctx) {
     c->cancel.store(1);
     return RT_OK;
 }
+int rt_set_traversal(void* ctx, int mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || (mode != RT_TRAVERSAL_EXACT && mode != RT_TRAVERSAL_WIDE)) return RT_ERR_INVALID_ARG;
+    c->traversal = mode;
+    return RT_OK;
+}
+int rt_get_traversal(void* ctx, int* effective) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !effective) return RT_ERR_INVALID_ARG;
+    *effective = c->traversal == RT_TRAVERSAL_WIDE && c->has_scene && c->view.wide_ok ? RT_TRAVERSAL_WIDE
+                                                                                     : RT_TRAVERSAL_EXACT;
+    return RT_OK;
+}
 
 /* test hook (not part of radiantium.h): builds the SAH tree of n primitive
  * boxes (6 floats each) on the host exactly as rt_upload_scene does and
@@ -1689,6 +1763,41 @@ int rt_debug_bvh(const float* boxes, int n, int max_prims, int64_t* node_count, 
     }
 }
 
+/* test hook (not part of radiantium.h): the wide tree of the fast traversal
+ * built from the host builder's tree of `boxes` (rtb::build_wide), one record
+ * per wide node: p (3 floats), e (3 bytes), nchild, qlo / qhi (3 x 8 bytes
+ * each, [axis][child]), child (8 binary node indices), wchild (8 wide indices
+ * or -1).  Call with NULL arrays to query the node count. */
+int rt_debug_wide(const float* boxes, int n, int max_prims, int64_t* node_count, float* p, uint8_t* e, uint8_t* nchild,
+                  uint8_t* qlo, uint8_t* qhi, int32_t* child, int32_t* wchild, int32_t* max_push) {
+    if (!boxes || n <= 0 || !node_count) return RT_ERR_INVALID_ARG;
+    try {
+        std::vector<rtb::Box> b(n);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) { b[i].mn[k] = boxes[6 * i + k]; b[i].mx[k] = boxes[6 * i + 3 + k]; }
+        rtb::BuildResult r = rtb::build_sah(b, max_prims, std::max(1u, std::thread::hardware_concurrency()));
+        rtb::WideResult w = rtb::build_wide(r);
+        *node_count = (int64_t)w.nodes.size();
+        if (max_push) *max_push = w.max_push;
+        if (!p) return RT_OK;
+        for (size_t i = 0; i < w.nodes.size(); i++) {
+            const rtb::WideNode& d = w.nodes[i];
+            for (int a = 0; a < 3; a++) {
+                p[3 * i + a] = d.p[a];
+                e[3 * i + a] = d.e[a];
+                std::memcpy(qlo + 24 * i + 8 * a, d.qlo[a], 8);
+                std::memcpy(qhi + 24 * i + 8 * a, d.qhi[a], 8);
+            }
+            nchild[i] = d.nchild;
+            std::memcpy(child + 8 * i, d.child, 32);
+            std::memcpy(wchild + 8 * i, d.wchild, 32);
+        }
+        return RT_OK;
+    } catch (...) {
+        return RT_ERR_OOM;
+    }
+}
+
 /* test hook (not part of radiantium.h): the GPU builder's tree in rt_debug_bvh's layout */
 int rt_debug_bvh_gpu(void* ctx, const float* boxes, int n, int max_prims, int64_t* node_count, float* bounds,
                      int32_t* idx, int32_t* count, int32_t* axis, int32_t* order, int32_t* depth) {
@@ -1716,6 +1825,14 @@ int rt_debug_bvh_gpu(void* ctx, const float* boxes, int n, int max_prims, int64_
 int rt_debug_device_allocations(unsigned long long* out) {
     if (!out) return RT_ERR_INVALID_ARG;
     *out = g_device_allocs.load(std::memory_order_relaxed);
+    return RT_OK;
+}
+/* test hook (not part of radiantium.h): the wavefront's bounce-iteration cap
+ * per round (0 restores WF_ITER_CAP), so a test can make it run out */
+int rt_debug_set_iter_cap(void* ctx, int cap) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || cap < 0) return RT_ERR_INVALID_ARG;
+    c->wf_iter_cap = cap == 0 ? WF_ITER_CAP : cap;
     return RT_OK;
 }
 /* test hook: primitive count from which upload_scene builds trees on the GPU */

@@ -9,7 +9,9 @@
 
 namespace rtd {
 
-#define RT_LOOP_CAP (1 << 16)
+#ifndef RT_LOOP_CAP
+#define RT_LOOP_CAP (1 << 16)          /* bounces of one path (the reference's loops have no cap) */
+#endif
 
 DF V3 Lo(const Isect& it, V3 v) { return ToLocal(it.F, v); }
 DF V3 Wo(const Isect& it, V3 v) { return ToWorld(it.F, v); }

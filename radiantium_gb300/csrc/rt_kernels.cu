@@ -81,6 +81,7 @@ DF Ray ray_from(const rt_ray& r) {
     return mkray(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), r.min_t, r.max_t);
 }
 
+template <bool kWide>
 __global__ void __launch_bounds__(128) k_trace_closest(const RtSceneView* __restrict__ S, const rt_ray* __restrict__ rays, int64_t n,
                                                          rt_hit* __restrict__ hits, uint32_t* status,
                                                          unsigned long long* stats, bool counting) {
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(const RtSceneView* __rest
     Ray r = ray;
     Best b;
     rt_hit h;
-    if (SceneClosest(S, r, &b, stack, status, counting ? &st : nullptr)) {
+    if (SceneClosest<kWide>(S, r, &b, stack, status, counting ? &st : nullptr)) {
         Isect it;
         Finish(S, ray, b, &it);
         h.t = it.T; h.u = it.bu; h.v = it.bv; h.prim = it.prim; h.sub = it.sub; h.flags = it.flags;
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(const RtSceneView* __rest
     }
 }
 
+template <bool kWide>
 __global__ void __launch_bounds__(128) k_trace_any(const RtSceneView* __restrict__ S, const rt_ray* __restrict__ rays, int64_t n,
                                                      uint8_t* __restrict__ occ, uint32_t* status,
                                                      unsigned long long* stats, bool counting) {
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(128) k_trace_any(const RtSceneView* __restrict
     int2 stack[2 * RT_STACK_SIZE];
     TravStats st = {0, 0, 0};
     Ray ray = ray_from(rays[i]);
-    occ[i] = SceneAny(S, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
+    occ[i] = SceneAny<kWide>(S, ray, stack, status, counting ? &st : nullptr) ? 1 : 0;
     if (counting) {
         warp_add(stats + 3, st.nodes);
         warp_add(stats + 4, st.prims);
@@ -174,11 +176,14 @@ cudaError_t rt_launch_finalize(float* out, const float* film, int64_t npix, floa
 }
 
 cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ,
-                            uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream) {
+                            uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream,
+                            bool wide) {
     if (n <= 0) return cudaSuccess;
     const int block = 128;
-    if (hits) k_trace_closest<<<grid_for(n, block), block, 0, stream>>>(S, rays, n, hits, status, stats, counting);
-    else k_trace_any<<<grid_for(n, block), block, 0, stream>>>(S, rays, n, occ, status, stats, counting);
+    if (hits && wide) k_trace_closest<true><<<grid_for(n, block), block, 0, stream>>>(S, rays, n, hits, status, stats, counting);
+    else if (hits) k_trace_closest<false><<<grid_for(n, block), block, 0, stream>>>(S, rays, n, hits, status, stats, counting);
+    else if (wide) k_trace_any<true><<<grid_for(n, block), block, 0, stream>>>(S, rays, n, occ, status, stats, counting);
+    else k_trace_any<false><<<grid_for(n, block), block, 0, stream>>>(S, rays, n, occ, status, stats, counting);
     return cudaGetLastError();
 }
 

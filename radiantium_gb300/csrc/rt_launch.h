@@ -14,7 +14,8 @@ cudaError_t rt_launch_render(const RtSceneView* S, const RtParams& P, float* sam
 cudaError_t rt_launch_accumulate(float* film, const float* samples, int64_t npix, int chunk_len, cudaStream_t stream);
 cudaError_t rt_launch_finalize(float* out, const float* film, int64_t npix, float spp, cudaStream_t stream);
 cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n, rt_hit* hits, uint8_t* occ,
-                            uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
+                            uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream,
+                            bool wide = false);
 /* device address of the fixed RT_NOALLOC_SCRATCH_BYTES scratch array on
  * `device`, which must be the current device; looked up once per device and
  * process (rt_noalloc.cu) */

@@ -663,13 +663,17 @@ DF bool IsOccluded(Ctx& c, V3 from, V3 to) {
     V3 dir = Normalize(vec);
     return SceneIntersectP(c, mkray(from, dir, 0.0001f, dis - 0.0001f));
 }
-#define RT_WALK_CAP 4096
-/* Scene.Transmittance (Scene.cs:72-103) */
+#ifndef RT_WALK_CAP
+#define RT_WALK_CAP 4096               /* segments of one null-boundary walk */
+#endif
+/* Scene.Transmittance (Scene.cs:72-103); a walk that reaches RT_WALK_CAP
+ * segments stops and reports RT_STATUS_WALK */
 DF C3 Transmittance(Ctx& c, V3 from, V3 to, int rayEnv) {
     C3 tr = c3s(1.0f);
     V3 start = from;
     V3 dir = Normalize(to - start);
-    for (int it = 0; it < RT_WALK_CAP; it++) {
+    for (int it = 0;; it++) {
+        if (it == RT_WALK_CAP) { atomicOr(c.status, RT_STATUS_WALK); break; }
         V3 vec = to - start;
         float dis = Length(vec);
         if (dis < 0.0001f) break;
@@ -687,7 +691,8 @@ DF C3 Transmittance(Ctx& c, V3 from, V3 to, int rayEnv) {
 /* Scene.IntersectTr (Scene.cs:105-131) */
 DF bool IntersectTr(Ctx& c, Ray ray, int rayEnv, Isect* inct, C3* tr) {
     *tr = c3s(1.0f);
-    for (int it = 0; it < RT_WALK_CAP; it++) {
+    for (int it = 0;; it++) {
+        if (it == RT_WALK_CAP) { atomicOr(c.status, RT_STATUS_WALK); break; }
         bool anyHit = SceneIntersect(c, ray, inct);
         if (!anyHit) {
             if (rayEnv >= 0) *tr = *tr * MedTr(c.S->media[rayEnv], ray);

@@ -33,6 +33,9 @@
 #define RT_STATUS_ITER 2u
 #define RT_STATUS_BADREF 4u
 #define RT_STATUS_BOUNDS 8u         /* debug-bounds builds: an index left its buffer, the access was skipped */
+#define RT_STATUS_TRAV 16u          /* a traversal reached RT_TRAVERSAL_CAP steps */
+#define RT_STATUS_WALK 32u          /* a null-boundary walk reached RT_WALK_CAP segments */
+#define RT_STATUS_WFITER 64u        /* a graph-driven wavefront round reached WF_ITER_CAP iterations */
 
 #define RT_LIGHT_AREA_TRI 0
 #define RT_LIGHT_AREA_SPHERE 1
@@ -43,8 +46,16 @@ struct RtBvh {
     float root_min[3];
     float root_max[3];
     int32_t root_ref;   /* >= 0: interior node (absolute), < 0: ~first slot of a root leaf, INT32_MIN: empty */
-    int32_t pad;
+    int32_t wide_root;  /* the same tree collapsed 8-wide: >= 0 wide node, < 0 as root_ref */
 };
+
+/* a wide node (the opt-in fast traversal; rtb::WideNode): float4 w0..w5
+ *   w0 = (p.x, p.y, p.z, uint e.x | e.y << 8 | e.z << 16 | nchild << 24)
+ *   w1 = (qlo.x of children 0-3, 4-7, qhi.x of 0-3, 4-7)   one byte per child
+ *   w2, w3: the same for y and z
+ *   w4 = (int ref 0..3), w5 = (int ref 4..7)   refs as in the binary tree
+ * the quantised child box of axis a is [p + qlo * s, p + qhi * s], s = 2^(e - 127) */
+#define RT_WIDE_F4 6
 
 /* an interior node: float4 n0..n3
  *   n0 = (L.min.x, L.min.y, L.min.z, L.max.x)
@@ -163,6 +174,9 @@ struct RtSceneView {
     int32_t deep_trees;         /* a tree is taller than RT_STACK_SIZE + 1 levels: its
                                  * traversal may overflow the stack, so every far child
                                  * is pushed exactly as the reference pushes it */
+    const float4* wnodes;       /* wide nodes of every tree (RT_WIDE_F4 float4 each) */
+    int32_t wide_ok;            /* every wide traversal fits the stack: the fast mode may run */
+    int32_t pad_;
     RtCamera camera;
 };
 

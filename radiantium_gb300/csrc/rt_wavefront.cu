@@ -312,8 +312,14 @@ template <> struct TraceStack<true> {
     }
 };
 
-/* closest-hit rays: extension and MIS rays (queue [0, n_closest)) */
-template <bool kSh>
+/* wide nodes per traversal step of the fast traversal (kWide) */
+#ifndef RT_DESCEND_WIDE
+#define RT_DESCEND_WIDE 1        /* C2 M samples/s: 154.7 at 1, 134.9 at 2, 120.5 at 3 */
+#endif
+
+/* closest-hit rays: extension and MIS rays (queue [0, n_closest)); kWide: the
+ * opt-in fast traversal over the wide nodes */
+template <bool kSh, bool kWide>
 __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_CLOSEST_BLOCKS) k_wf_trace_closest(WfState W, uint32_t* status, unsigned long long* stats,
                                                             bool counting) {
     const int n = min(W.ctr->n_closest, 2 * W.slots);
@@ -335,11 +341,12 @@ __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_CLOSEST_BLOCKS) k_wf_trace_
             if (item < 0 && q < n) {
                 meta = W.q_meta[q];
                 S = W.jobs[meta_job(meta)].view;
-                if (ClosestBegin(S, queued_ray(W, q), T, pst)) { closest_done(W, meta, T); done++; }
+                if (ClosestBegin<kWide>(S, queued_ray(W, q), T, pst)) { closest_done(W, meta, T); done++; }
                 else item = q;
             }
         }
-        if (item >= 0 && ClosestStep<decltype(stack), kSh ? RT_DESCEND_DEEP : RT_DESCEND>(S, T, stack, status, pst)) {
+        if (item >= 0 && ClosestStep<decltype(stack), kWide ? RT_DESCEND_WIDE : (kSh ? RT_DESCEND_DEEP : RT_DESCEND), kWide>(
+                             S, T, stack, status, pst)) {
             closest_done(W, meta, T);
             done++;
             item = -1;
@@ -368,7 +375,7 @@ DF void shadow_done(const WfState& W, int meta, bool hit) {
 }
 
 /* shadow rays: any-hit (queue [shadow_base, shadow_base + n_shadow)) */
-template <bool kSh>
+template <bool kSh, bool kWide>
 __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_SHADOW_BLOCKS) k_wf_trace_shadow(WfState W, uint32_t* status, unsigned long long* stats,
                                                            bool counting) {
     const int n = min(W.ctr->n_shadow, W.slots);
@@ -391,11 +398,12 @@ __global__ void __launch_bounds__(RT_TRACE_BLOCK, RT_SHADOW_BLOCKS) k_wf_trace_s
                 const int q = W.shadow_base + e;
                 meta = W.q_meta[q];
                 S = W.jobs[meta_job(meta)].view;
-                if (AnyBegin(S, queued_ray(W, q), T, pst)) { shadow_done(W, meta, false); done++; }
+                if (AnyBegin<kWide>(S, queued_ray(W, q), T, pst)) { shadow_done(W, meta, false); done++; }
                 else item = q;
             }
         }
-        if (item >= 0 && AnyStep<decltype(stack), kSh ? RT_DESCEND_DEEP : RT_DESCEND>(S, T, stack, status, pst)) {
+        if (item >= 0 && AnyStep<decltype(stack), kWide ? RT_DESCEND_WIDE : (kSh ? RT_DESCEND_DEEP : RT_DESCEND), kWide>(
+                             S, T, stack, status, pst)) {
             shadow_done(W, meta, T.hit);
             done++;
             item = -1;
@@ -779,7 +787,7 @@ DF bool trw_step(const RtSceneView* S, const WfState& W, int slot) {
         else {
             start = inct.P;
             env = GetMedium(S, inct, dir);
-            if (++count >= RT_WALK_CAP) more = false;
+            if (++count >= RT_WALK_CAP) { more = false; atomicOr(W.status, RT_STATUS_WALK); }
         }
     }
     W.trw_tr[slot] = make_float4(tr.r, tr.g, tr.b, 0.0f);
@@ -813,6 +821,7 @@ DF bool itw_step(const RtSceneView* S, const WfState& W, int slot, int light, V3
             if (LightOf(S, inct) >= 0 && LightOf(S, inct) == light) li = IsectLe(S, inct, wle);
         } else if (++count >= RT_WALK_CAP) {
             li = EvalAllInfinite(S, ray.D);             /* the walk gives up: a miss */
+            atomicOr(W.status, RT_STATUS_WALK);
         } else {
             ray = mkray(inct.P, ray.D, 0.001f);
             env = GetMedium(S, inct, ray.D);
@@ -1463,7 +1472,7 @@ __global__ void k_wf_tail_loop(WfState W, cudaGraphConditionalHandle loop, uint3
         /* queued shadow rays keep the loop going: a finished light-tracer
          * particle leaves its last splat in the queue without an active slot */
         bool more = W.ctr->n_active[next] > 0 || W.ctr->n_shadow > 0;
-        if (more && W.ctr->iter >= WF_ITER_CAP) { atomicOr(status, RT_STATUS_ITER); more = false; }
+        if (more && W.ctr->iter >= W.iter_cap) { atomicOr(status, RT_STATUS_WFITER); more = false; }
         cudaGraphSetConditional(loop, more ? 1u : 0u);
     }
 }
@@ -1492,17 +1501,30 @@ cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle) {
 }
 
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
-                        bool deep) {
-    static const int closest_blocks[2] = {resident_blocks(k_wf_trace_closest<false>, RT_TRACE_BLOCK),
-                                          resident_blocks(k_wf_trace_closest<true>, RT_TRACE_BLOCK)};
-    static const int shadow_blocks[2] = {resident_blocks(k_wf_trace_shadow<false>, RT_TRACE_BLOCK),
-                                         resident_blocks(k_wf_trace_shadow<true>, RT_TRACE_BLOCK)};
-    if (deep) k_wf_trace_closest<true><<<closest_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
-    else k_wf_trace_closest<false><<<closest_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
+                        bool deep, bool wide) {
+    static const int closest_blocks[4] = {resident_blocks(k_wf_trace_closest<false, false>, RT_TRACE_BLOCK),
+                                          resident_blocks(k_wf_trace_closest<true, false>, RT_TRACE_BLOCK),
+                                          resident_blocks(k_wf_trace_closest<false, true>, RT_TRACE_BLOCK),
+                                          resident_blocks(k_wf_trace_closest<true, true>, RT_TRACE_BLOCK)};
+    static const int shadow_blocks[4] = {resident_blocks(k_wf_trace_shadow<false, false>, RT_TRACE_BLOCK),
+                                         resident_blocks(k_wf_trace_shadow<true, false>, RT_TRACE_BLOCK),
+                                         resident_blocks(k_wf_trace_shadow<false, true>, RT_TRACE_BLOCK),
+                                         resident_blocks(k_wf_trace_shadow<true, true>, RT_TRACE_BLOCK)};
+    const int v = (deep ? 1 : 0) + (wide ? 2 : 0);
+    switch (v) {
+    case 0: k_wf_trace_closest<false, false><<<closest_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    case 1: k_wf_trace_closest<true, false><<<closest_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    case 2: k_wf_trace_closest<false, true><<<closest_blocks[2], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    default: k_wf_trace_closest<true, true><<<closest_blocks[3], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if (deep) k_wf_trace_shadow<true><<<shadow_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
-    else k_wf_trace_shadow<false><<<shadow_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting);
+    switch (v) {
+    case 0: k_wf_trace_shadow<false, false><<<shadow_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    case 1: k_wf_trace_shadow<true, false><<<shadow_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    case 2: k_wf_trace_shadow<false, true><<<shadow_blocks[2], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    default: k_wf_trace_shadow<true, true><<<shadow_blocks[3], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    }
     return cudaGetLastError();
 }
 

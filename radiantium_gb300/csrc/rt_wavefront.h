@@ -26,7 +26,9 @@ enum { WF_RAY_SPLAT = 2 };
 #define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
 #define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
 #define WF_SHADE_KEYS 256          /* shade key: (job mod 16) * 16 + the path's code key (0..15) */
+#ifndef WF_ITER_CAP
 #define WF_ITER_CAP (1 << 20)      /* bounce iterations of one round before a run gives up */
+#endif
 
 /* one render of a batch, for the current round of samples (light tracing:
  * `samples` is the film sums, one float4 per pixel, `first` the first
@@ -77,6 +79,7 @@ struct WfState {
     int32_t slots;
     uint32_t* status;        /* the context's status word (RT_STATUS_*) */
     int32_t refill;          /* idle lanes of a trace warp before it fetches new rays */
+    int32_t iter_cap;        /* bounce iterations of one round before the run gives up (WF_ITER_CAP) */
     WfCounters* ctr;
     const WfJob* jobs;
     /* active slot lists by iteration parity, and the list regrouped by shade key */
@@ -123,12 +126,13 @@ struct WfState {
 cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false);
 /* Traces the queued closest-hit and shadow rays (lengths read on the device);
  * `deep`: a tree of the scene has RT_DEEP_TREE levels or more, the kernels
- * keep the bottom of the traversal stack in shared memory. */
+ * keep the bottom of the traversal stack in shared memory.  `wide`: the
+ * opt-in fast traversal over the scenes' wide nodes. */
 #ifndef RT_DEEP_TREE
 #define RT_DEEP_TREE 16
 #endif
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
-                        bool deep = false);
+                        bool deep = false, bool wide = false);
 /* Shades the active paths (`particle`: light-tracer particles) - regrouped by
  * shade key first with `sort` - then advances the iteration; with `loop` set
  * (inside a captured while-loop), also sets the loop's condition to "paths

@@ -64,6 +64,16 @@ class Device:
         """N.RENDERER_AUTO / RENDERER_MEGAKERNEL / RENDERER_WAVEFRONT"""
         self._check(self.lib.rt_set_renderer(self.h, mode))
 
+    def set_traversal(self, mode: int):
+        """N.TRAVERSAL_EXACT (the reference's tree and order) / N.TRAVERSAL_WIDE (opt-in fast traversal)"""
+        self._check(self.lib.rt_set_traversal(self.h, mode))
+
+    def traversal(self) -> int:
+        """The traversal the next call will run (WIDE only where the uploaded scene allows it)."""
+        v = C.c_int()
+        self._check(self.lib.rt_get_traversal(self.h, C.byref(v)))
+        return v.value
+
     def stats(self) -> dict:
         st = N.Stats()
         self._check(self.lib.rt_get_stats(self.h, C.byref(st)))

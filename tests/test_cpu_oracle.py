@@ -312,3 +312,72 @@ def test_particle_tracer_agrees_with_path_tracer():
     m = ref.max(axis=2) < 2
     a, b = img[m].mean(axis=0), ref[m].mean(axis=0)
     assert np.all(np.abs(a / b - 1) < 0.06), (a, b)
+
+
+# ---- the wide tree of the fast traversal (rtb::build_wide) ---------------------------------------
+def _lib_wide(boxes, max_prims=1):
+    lib = N.load_library()
+    f = lib.rt_debug_wide
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int64)] + [C.c_void_p] * 7 + [C.POINTER(C.c_int32)]
+    boxes = np.ascontiguousarray(boxes, dtype=np.float32)
+    nn, push = C.c_int64(), C.c_int32()
+    assert f(boxes.ctypes.data, boxes.shape[0], max_prims, C.byref(nn), *([None] * 7), C.byref(push)) == 0
+    n = nn.value
+    w = {"p": np.zeros((n, 3), np.float32), "e": np.zeros((n, 3), np.uint8), "nchild": np.zeros(n, np.uint8),
+         "qlo": np.zeros((n, 3, 8), np.uint8), "qhi": np.zeros((n, 3, 8), np.uint8),
+         "child": np.zeros((n, 8), np.int32), "wchild": np.zeros((n, 8), np.int32)}
+    assert f(boxes.ctypes.data, boxes.shape[0], max_prims, C.byref(nn), *(w[k].ctypes.data for k in
+             ("p", "e", "nchild", "qlo", "qhi", "child", "wchild")), C.byref(push)) == 0
+    w["max_push"] = push.value
+    return w
+
+
+@pytest.mark.parametrize("case", ["sphere", "duplicates", "flat", "cornell"])
+def test_wide_tree_covers_the_binary_tree(ensure_lib, case):
+    """Every leaf of the binary tree is a child of exactly one wide node, every
+    interior child is expanded exactly once, and each quantised child box
+    contains the child's exact box with at least one grid step to spare on
+    every side (outward rounding: the fast traversal cannot miss a box the
+    exact slab test accepts)."""
+    if case == "sphere":
+        boxes = _tri_boxes(procedural.displaced_sphere(40, 5))
+    elif case == "duplicates":
+        rng = np.random.default_rng(4)
+        lo = rng.random((2000, 3)).astype(np.float32)
+        lo[500:900] = lo[500]
+        boxes = np.concatenate([lo, lo + 0.01], axis=1)
+    elif case == "flat":
+        rng = np.random.default_rng(5)
+        lo = rng.random((1500, 3)).astype(np.float32) * 100
+        lo[:, 1] = 3.0                                             # every box on the plane y = 3
+        boxes = np.concatenate([lo, lo + np.array([0.5, 0.0, 0.5], np.float32)], axis=1)
+    else:
+        s, _ = procedural.cornell_box(16, 16)
+        boxes = np.concatenate([_tri_boxes(m) for m in s.meshes])
+    b = _lib_bvh(boxes)
+    w = _lib_wide(boxes)
+    nb = b["count"].size
+    seen = np.zeros(nb, np.int32)
+    for i in range(w["nchild"].size):
+        k = int(w["nchild"][i])
+        assert 2 <= k <= 8
+        s = np.ldexp(1.0, w["e"][i].astype(np.int64) - 127)
+        for c in range(k):
+            bn = w["child"][i, c]
+            seen[bn] += 1
+            assert (b["count"][bn] == 0) == (w["wchild"][i, c] >= 0)
+            lo = w["p"][i].astype(np.float64) + w["qlo"][i, :, c] * s
+            hi = w["p"][i].astype(np.float64) + w["qhi"][i, :, c] * s
+            ex_lo = b["bounds"][bn, :3].astype(np.float64)
+            ex_hi = b["bounds"][bn, 3:].astype(np.float64)
+            assert (lo + s <= ex_lo).all() and (hi - s >= ex_hi).all(), (i, c, lo, ex_lo, hi, ex_hi)
+        for c in range(k, 8):
+            assert (w["qlo"][i, :, c] > w["qhi"][i, :, c]).all()
+    leaves = b["count"] > 0
+    assert (seen[leaves] == 1).all()
+    interior = np.nonzero(~leaves)[0]
+    # every interior binary node is either a wide node's root or collapsed into one: the roots are
+    # the interior children plus the tree root; all leaves are reached, so the cover is complete
+    assert seen[0] == 0 and w["nchild"].size <= interior.size
+    assert 0 <= w["max_push"] <= 7 * w["nchild"].size

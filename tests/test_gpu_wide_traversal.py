@@ -1,0 +1,159 @@
+"""The opt-in fast traversal (RT_TRAVERSAL_WIDE) against the exact one (gpu).
+
+The exact traversal is the reference's tree in the reference's order and is
+shown equal to the oracle elsewhere; the fast one collapses the same trees
+8-wide with quantised, outward-rounded child boxes.  Its contract, as the
+tolerance for this path states it:
+
+  * hit primitive ids equal the exact traversal's, with t, u, v bit for bit
+    (the same Moller-Trumbore arithmetic on the same primitive), except where
+    (a) two candidates are within 4 ulp of each other - exactly equal t
+        (a tie), or coplanar surfaces a ulp apart of which the reference's
+        box test culled the second at rounding scale - which the fast
+        traversal meets and flags RT_HIT_TIE; the hit distance then stays
+        within 4 ulp of the exact one, or
+    (b) the fast traversal finds a hit more than 4 ulp closer: a primitive
+        whose box the reference's slab test rejected at rounding scale (the
+        fast boxes are conservative);
+    the fast hit is never farther than the exact one; ties stay under 1 % of
+    the rays (coplanar light and ceiling, boxes standing on the floor) and
+    (b) under 1 in 10,000;
+  * any-hit answers are a superset of the exact ones (the same reason);
+  * films differ from the exact films only in the paths that met such a ray:
+    almost every float is identical and the relative mean squared difference
+    is tiny.
+Rays: 1 M per benchmark scene (camera rays and random rays through the
+scene's box), 200 k for the small scenes.
+"""
+import numpy as np
+import pytest
+
+from radiantium_gb300 import native as N
+from radiantium_gb300 import procedural
+from oracle.oracle import OracleScene
+from tests.test_gpu_parity import random_rays
+
+pytestmark = pytest.mark.gpu
+
+MAX_TIES = 1e-2         # rays whose hit is one of two candidates within 4 ulp
+MAX_MISSES = 1e-4       # rays where the reference's slab test missed a closer hit
+TIE_ULP = 4
+
+
+def _scene(name):
+    return {"cornell": lambda: procedural.cornell_box(256, 256),
+            "zoo": lambda: procedural.material_zoo(64, 64),
+            "C2": procedural.instanced_spheres,
+            "C3": procedural.volume_sphere,
+            "C4": lambda: procedural.batch_scene(8)}[name]()
+
+
+def _rays(s, n, seed):
+    orc = OracleScene(s)
+    try:
+        rng = np.random.default_rng(seed)
+        cam = s.camera
+        cam_rays = orc.camera_rays(rng.random((n // 2, 2)) * np.array([cam.width, cam.height]))
+        root = orc.bvh(-1)["bounds"][0].astype(np.float64)
+    finally:
+        orc.close()
+    box = (root[:3], root[3:])
+    return np.concatenate([cam_rays, random_rays(box, n // 4, seed + 1),
+                           random_rays(box, n - n // 2 - n // 4, seed + 2, inside=True)])
+
+
+def _trace(dev, rays, mode):
+    dev.set_traversal(mode)
+    try:
+        assert dev.traversal() == mode
+        return dev.trace_closest(rays), dev.trace_any(rays)
+    finally:
+        dev.set_traversal(N.TRAVERSAL_EXACT)
+
+
+@pytest.mark.parametrize("name", ["cornell", "zoo", "C2", "C3", "C4"])
+def test_wide_hits_equal_exact_up_to_ties_and_slab_misses(dev, name):
+    s, _ = _scene(name)
+    dev.upload(s)
+    n = 1 << 20 if name in ("C2", "C3") else 200000
+    rays = _rays(s, n, 7)
+    e, ea = _trace(dev, rays, N.TRAVERSAL_EXACT)
+    w, wa = _trace(dev, rays, N.TRAVERSAL_WIDE)
+    same = (e["prim"] == w["prim"]) & (e["sub"] == w["sub"])
+    # the same primitive: the same arithmetic
+    for k in ("t", "u", "v"):
+        assert np.array_equal(e[k][same].view(np.uint32), w[k][same].view(np.uint32)), k
+    diff = ~same
+    et, wt = e["t"][diff], w["t"][diff]
+    hit_e = e["prim"][diff] >= 0
+    # never farther, never a miss where the exact traversal hits
+    assert (w["prim"][diff][hit_e] >= 0).all()
+    assert (wt[hit_e] <= et[hit_e]).all()
+    ulp = np.abs(et.view(np.int32).astype(np.int64) - wt.view(np.int32).astype(np.int64))
+    tie = hit_e & (ulp <= TIE_ULP)
+    assert ((w["flags"][diff] & N.HIT_TIE) != 0)[tie].all(), "a tie is flagged"
+    ties, misses = int(tie.sum()), int(diff.sum()) - int(tie.sum())
+    print(f"{name}: {rays.size} rays, {ties} ties (within {TIE_ULP} ulp), {misses} reference slab misses")
+    assert ties <= MAX_TIES * rays.size, (name, ties)
+    assert misses <= MAX_MISSES * rays.size, (name, misses)
+    # any hit: a superset of the exact answers
+    assert not (ea.astype(bool) & ~wa.astype(bool)).any()
+    assert int((wa.astype(bool) & ~ea.astype(bool)).sum()) <= MAX_MISSES * rays.size
+    assert (e["prim"] >= 0).sum() > rays.size // 10
+
+
+@pytest.mark.parametrize("name,spp", [("C2", 2), ("C3", 2), ("zoo", 16)])
+def test_wide_films_match_exact(dev, name, spp):
+    s, st = _scene(name)
+    dev.upload(s)
+    st = st.replace(spp=spp, sample_begin=3)
+    if name == "C2":
+        st = st.replace(x0=256, y0=256, width=512, height=512)
+    films = []
+    for mode in (N.TRAVERSAL_EXACT, N.TRAVERSAL_WIDE):
+        dev.set_traversal(mode)
+        try:
+            films.append(dev.render(st))
+        finally:
+            dev.set_traversal(N.TRAVERSAL_EXACT)
+    a, b = films
+    assert np.isfinite(b).all()
+    same = np.mean(a.view(np.uint32) == b.view(np.uint32))
+    rel = float((((a.astype(np.float64) - b) ** 2) / (a.astype(np.float64) ** 2 + 1e-2)).mean())
+    assert same >= 0.99, (name, same)
+    assert rel <= 1e-4, (name, rel)
+
+
+def test_wide_batch_equals_each_scene(dev):
+    """A batch under the fast traversal reproduces each scene's own fast render."""
+    from radiantium_gb300.device import Device
+    scenes = [procedural.batch_scene(i) for i in (0, 3, 8)]
+    devs = []
+    try:
+        for sc, _ in scenes:
+            d = Device(0)
+            d.upload(sc)
+            d.set_traversal(N.TRAVERSAL_WIDE)
+            devs.append(d)
+        host = Device(0)
+        host.set_traversal(N.TRAVERSAL_WIDE)
+        items = [(d, st.replace(spp=1, sample_begin=2)) for d, (_, st) in zip(devs, scenes)]
+        films = host.render_batch(items)
+        for (d, st), f in zip(items, films):
+            assert np.array_equal(f.view(np.uint32), d.render(st).view(np.uint32))
+        host.close()
+    finally:
+        for d in devs:
+            d.close()
+
+
+def test_traversal_mode_arguments(dev):
+    s, _ = _scene("cornell")
+    dev.upload(s)
+    with pytest.raises(N.RTError) as e:
+        dev.set_traversal(7)
+    assert e.value.code == N.RT_ERR_INVALID_ARG
+    assert dev.traversal() == N.TRAVERSAL_EXACT
+    dev.set_traversal(N.TRAVERSAL_WIDE)
+    assert dev.traversal() == N.TRAVERSAL_WIDE
+    dev.set_traversal(N.TRAVERSAL_EXACT)
