@@ -831,7 +831,13 @@ void render_megakernel(Ctx* c, RtParams P, int chunk, int64_t npix, cudaStream_t
     ensure_events(c, 2 * (size_t)nchunks);
     uint64_t launches = 0;
     for (int b = 0, ci = 0; b < P.spp; b += chunk, ci++) {
-        if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        /* at most two chunks queued, so a cancel from another thread takes
+         * effect within a chunk or two (Renderer.Stop) */
+        if (ci >= 2) CK(cudaEventSynchronize(c->events[2 * (ci - 2) + 1]));
+        if (c->cancel.load()) {
+            cudaStreamSynchronize(s);
+            throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+        }
         P.chunk_begin = b;
         P.chunk_len = std::min(chunk, P.spp - b);
         CK(cudaEventRecord(c->events[2 * ci], s));
@@ -1006,7 +1012,11 @@ void render_particles(Ctx* c, const rt_render_params* p, int64_t first, int64_t 
     if (mega) {
         ensure_events(c, 2 * (size_t)nchunks);
         for (int64_t b = 0, ci = 0; b < count; b += chunk, ci++) {
-            if (c->cancel.load()) throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+            if (ci >= 2) CK(cudaEventSynchronize(c->events[2 * (ci - 2) + 1]));
+            if (c->cancel.load()) {
+                cudaStreamSynchronize(s);
+                throw RtFail(RT_ERR_CANCELLED, "render cancelled");
+            }
             CK(cudaEventRecord(c->events[2 * ci], s));
             CK(rt_launch_particles(c->d_view, P, first + b, std::min(chunk, count - b), film, c->status, c->stats,
                                    c->counting, s));
