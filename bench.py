@@ -413,6 +413,11 @@ def run_ours(args):
                        f"{upload_s:.2f} s incl. BVH builds); h2d = the job tables and queue counters the "
                        "call copies (rt_stats.h2d_bytes)"}
 
+    # the opt-in wide traversal on the same passes (the headline stays on the exact one)
+    wide = None
+    if uses_wavefront and traversal == N.TRAVERSAL_EXACT and not args.no_subrecords and rank == 0:
+        wide = wide_subrecord(dev, st, spp_step, base + args.warmup * spp_step, film, flush, stream, value, ms_step)
+
     # the plain megakernel on the same passes, for the wavefront / megakernel ratio
     plain = None
     if uses_wavefront and args.plain_steps > 0:
@@ -485,6 +490,7 @@ def run_ours(args):
                      "limiter_source": (f"profiles/trace_{args.workload}_traffic.txt (ncu --set full, one launch of "
                                         "k_wf_trace_closest)") if l2f is not None else None},
         "plain_megakernel": plain,
+        "wide_traversal": wide,
         "relmse": relmse,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -503,6 +509,48 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def wide_subrecord(dev, st, spp_step, begin, film, flush, stream, exact_value, exact_ms, steps=4, warmup=2):
+    """The same passes with the opt-in wide traversal (RT_TRAVERSAL_WIDE): its
+    samples/s against the exact traversal's, and how far one pass's film is
+    from the exact film (share of identical floats, relative mean squared
+    difference)."""
+    import torch
+    from radiantium_gb300 import native as N
+    dev.set_traversal(N.TRAVERSAL_WIDE)
+    if dev.traversal() != N.TRAVERSAL_WIDE:
+        dev.set_traversal(N.TRAVERSAL_EXACT)
+        return {"available": False, "note": "the scene's wide trees could overflow the traversal stack"}
+    try:
+        for i in range(warmup):
+            dev.render_device(st.replace(spp=spp_step, sample_begin=begin + i * spp_step), film.data_ptr(), stream)
+        torch.cuda.synchronize()
+        times, trace = [], 0.0
+        for i in range(steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.render_device(st.replace(spp=spp_step, sample_begin=begin + i * spp_step), film.data_ptr(), stream)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            trace += dev.stats()["render_kernel_ms"]
+        ms = float(np.mean(times))
+        wide_film = film.clone()
+    finally:
+        dev.set_traversal(N.TRAVERSAL_EXACT)
+    dev.render_device(st.replace(spp=spp_step, sample_begin=begin + (steps - 1) * spp_step), film.data_ptr(), stream)
+    torch.cuda.synchronize()
+    a, b = film.double(), wide_film.double()
+    value = exact_value * exact_ms / ms
+    return {"available": True, "value": value, "unit": "samples/s", "steps": steps, "ms_per_step": ms,
+            "trace_ms_per_step": trace / steps, "vs_exact": value / exact_value,
+            "identical_floats": float((film.view(torch.int32) == wide_film.view(torch.int32)).double().mean().item()),
+            "relmse_vs_exact": float((((b - a) ** 2) / (a ** 2 + 1e-2)).mean().item()),
+            "note": "rt_set_traversal(RT_TRAVERSAL_WIDE): the same trees collapsed 8-wide with quantised child boxes; "
+                    "hits equal the exact traversal's up to ties within 4 ulp and rounding-scale box culls of the "
+                    "reference (tests/test_gpu_wide_traversal.py)"}
 
 
 def batch_subrecord(args, rank, world, local, dist):
