@@ -346,8 +346,8 @@ int rt_get_stats(void* ctx, rt_stats* out);
 int rt_set_counting(void* ctx, int enabled);
 
 /* Selects the render pipeline: RT_RENDERER_AUTO (wavefront where it applies,
- * i.e. the `path` and `vol_path` integrators with the Uniform light
- * strategy, megakernel otherwise; vol_path and the light tracer drive their
+ * i.e. the `path` integrator with either light strategy and `vol_path` with
+ * the Uniform one, megakernel otherwise; vol_path and the light tracer drive their
  * wavefront loop as a CUDA graph), RT_RENDERER_MEGAKERNEL, RT_RENDERER_WAVEFRONT (bounce loop
  * driven by the host, with per-phase timings in rt_stats) or
  * RT_RENDERER_WAVEFRONT_GRAPH (bounce loop as one CUDA graph launch per
@@ -392,9 +392,9 @@ typedef struct rt_batch_item {
  * path slots and every trace / shade launch, so small scenes do not leave
  * the GPU idle and the launch overhead is paid once per bounce for the whole
  * batch.  Each film equals what rt_render gives for the same item, bit for
- * bit.  All items must use the same integrator (`path` or `vol_path`) with
- * the Uniform light strategy, and all scene contexts must be on the batch
- * context's device.
+ * bit.  All items must use the same integrator (`path`, either light
+ * strategy, or `vol_path` with the Uniform one), and all scene contexts must
+ * be on the batch context's device.
  * The bounce loop is driven from the host, or runs as a CUDA graph when
  * rt_set_renderer selected RT_RENDERER_WAVEFRONT_GRAPH.  No counterpart in
  * the reference, which renders one scene per process

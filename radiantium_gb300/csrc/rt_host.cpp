@@ -204,6 +204,7 @@ void ensure_wf(Ctx* c, int slots) {
     W.pd_coeff = wf_alloc<float4>(c, n); W.pd_l1 = wf_alloc<float4>(c, n); W.pd_fr = wf_alloc<float4>(c, n);
     W.pd_mis = wf_alloc<float4>(c, n); W.pd_w = wf_alloc<float4>(c, n);
     W.pd_ray_o = wf_alloc<float4>(c, n); W.pd_ray_d = wf_alloc<float4>(c, n);
+    W.pd_acc = wf_alloc<float4>(c, n);
     W.ext_hit = wf_alloc<float4>(c, n); W.ext_sub = wf_alloc<int32_t>(c, n);
     W.mis_hit = wf_alloc<float4>(c, n); W.mis_sub = wf_alloc<int32_t>(c, n);
     W.occluded = wf_alloc<uint8_t>(c, n);
@@ -796,11 +797,12 @@ void render(Ctx* c, const rt_render_params* p, float* dst, bool dst_host, cudaSt
     CK(cudaMemsetAsync(c->status, 0, 4, s));
     CK(cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), s));
     c->cancel.store(0);
-    const bool uniform_path = P.strategy == RT_STRATEGY_UNIFORM;   /* path or vol_path */
+    /* the wavefront runs path with either light strategy, vol_path with Uniform */
+    const bool wf_ok = P.strategy == RT_STRATEGY_UNIFORM || P.integrator == RT_INTEGRATOR_PATH;
     const bool wavefront = c->renderer == RT_RENDERER_WAVEFRONT || c->renderer == RT_RENDERER_WAVEFRONT_GRAPH;
-    if (wavefront && !uniform_path)
-        throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs the Uniform light strategy");
-    if (wavefront || (c->renderer == RT_RENDERER_AUTO && uniform_path)) {
+    if (wavefront && !wf_ok)
+        throw RtFail(RT_ERR_UNSUPPORTED, "the wavefront renderer runs vol_path with the Uniform light strategy");
+    if (wavefront || (c->renderer == RT_RENDERER_AUTO && wf_ok)) {
         render_wavefront(c, P, chunk, npix, s);
     } else {
         render_megakernel(c, P, chunk, npix, s);
@@ -1314,8 +1316,9 @@ void render_batch(Ctx* c, const rt_batch_item* items, int n, bool device_out, cu
         if (!sc->has_scene) throw RtFail(RT_ERR_NO_SCENE, "render_batch: item " + std::to_string(i) + " has no uploaded scene");
         if (p->spp <= 0) throw RtFail(RT_ERR_INVALID_ARG, "render_batch: item " + std::to_string(i) + " has spp <= 0");
         if ((p->integrator != RT_INTEGRATOR_PATH && p->integrator != RT_INTEGRATOR_VOL_PATH) ||
-            p->strategy != RT_STRATEGY_UNIFORM || p->integrator != items[0].params.integrator)
-            throw RtFail(RT_ERR_UNSUPPORTED, "render_batch: items must share the path or vol_path integrator and use the Uniform light strategy");
+            (p->strategy != RT_STRATEGY_UNIFORM && p->integrator != RT_INTEGRATOR_PATH) ||
+            p->integrator != items[0].params.integrator)
+            throw RtFail(RT_ERR_UNSUPPORTED, "render_batch: items must share the path or vol_path integrator; vol_path items use the Uniform light strategy");
         RtParams P{};
         P.integrator = p->integrator; P.method = p->method; P.strategy = p->strategy;
         P.max_depth = p->max_depth; P.min_depth = p->min_depth; P.rr = p->rr_threshold;

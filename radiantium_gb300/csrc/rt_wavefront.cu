@@ -52,6 +52,7 @@ enum : uint32_t {
     F_WTR = 256u,        /* vol_path: a Transmittance-walk segment is being traced */
     F_WIT = 512u,        /* vol_path: an IntersectTr-walk segment is being traced */
     F_CONT = 1024u,      /* vol_path: the next extension ray waits for the pending term */
+    F_ALL = 2048u,       /* path, All light strategy: the vertex's lights are estimated one per iteration */
 };
 
 DF void warp_add64(unsigned long long* dst, uint32_t v) {
@@ -476,6 +477,93 @@ struct PathOut {
     bool shadow, mis, ext, keep, restart;
 };
 
+/* Schedules one light's direct term at vertex `it` (PathTracer.cs:309-399
+ * for Mis, :95-190 for Nee): draws its light sample and, for Mis, its BSDF
+ * sample, stores the term's parts and queues its shadow / MIS rays; the next
+ * shade adds it once they are traced.  lightPdf: SampleLight's pdf (Uniform)
+ * or 1 (All). */
+template <bool kAdj>
+DF void schedule_direct(PathOut* o, const WfState& W, const RtSceneView* S, int slot, const Isect& it, V3 wo, int mat,
+                        int light, float lightPdf, C3 coeff, int method, Rng& rand, uint32_t& fl, float4& rho) {
+    if (method == RT_METHOD_MIS) {
+        fl |= F_PENDING;
+        W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+        if (lightPdf > 0.0f) {
+            V3 wod = it.Wr;
+            LSample ls = LightSampleLi(S, light, it.P, rand);
+            if (ls.Pdf > 0.0f && !IsBlack(ls.Li)) {
+                C3 fr = MatFr(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                float scatteringPdf = MatPdf(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
+                if (!IsBlack(fr)) {
+                    /* IsOccluded(it.P, ls.P) */
+                    V3 vec = ls.P - it.P;
+                    float dis = Length(vec);
+                    if (!(dis < 0.001f)) {
+                        fr = fr * AbsCosTheta(Lo(it, ls.Wi));
+                        float weight = PowerHeuristic(ls.Pdf, scatteringPdf);
+                        if (kAdj && __float_as_int(rho.w) >= 0)
+                            rho.x = DirectDln(S, mat, Lo(it, wod), Lo(it, ls.Wi), weight, true, it.UV);
+                        C3 l1 = fr * ls.Li * weight / ls.Pdf;
+                        W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
+                        fl |= F_L1;
+                        ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
+                        o->shadow = true;
+                    }
+                }
+            }
+            BSample sample = MatSample(S, mat, Lo(it, wod), it.UV, rand);
+            C3 fr = sample.Fr * AbsCosTheta(sample.Wi);
+            float scatteringPdf = sample.Pdf;
+            bool sampledSpecular = (sample.Type & BX_SPECULAR) != 0;
+            if (!IsBlack(fr) && scatteringPdf > 0) {
+                float weight = 1;
+                bool go = true;
+                if (!sampledSpecular) {
+                    float bxdfToLightPdf = LightPdfLi(S, light, it.P, Wo(it, sample.Wi));
+                    if (bxdfToLightPdf == 0.0f) go = false;
+                    else weight = PowerHeuristic(scatteringPdf, bxdfToLightPdf);
+                }
+                if (go) {
+                    if (kAdj && __float_as_int(rho.w) >= 0)
+                        rho.y = DirectDln(S, mat, Lo(it, wod), sample.Wi, sampledSpecular ? 2.0f : weight, false,
+                                          it.UV);
+                    Ray toLight = Spawn(it, Wo(it, sample.Wi));
+                    V3 wle = Wo(it, -sample.Wi);
+                    W.pd_fr[slot] = make_float4(fr.r, fr.g, fr.b, weight);
+                    W.pd_mis[slot] = make_float4(scatteringPdf, __int_as_float(light), 0, 0);
+                    W.pd_w[slot] = make_float4(wle.x, wle.y, wle.z, 0);
+                    W.pd_ray_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
+                    W.pd_ray_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, toLight.MaxT);
+                    fl |= F_L2;
+                    o->mis = true;
+                }
+            }
+        } else {
+            fl |= F_DZERO;
+        }
+    } else { /* NEE: NeeEstimateLight */
+        if (lightPdf > 0.0f) {
+            fl |= F_PENDING;
+            W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
+            LSample r = LightSampleLi(S, light, it.P, rand);
+            bool zero = true;
+            if (r.Pdf > 0.0f) {
+                V3 vec = r.P - it.P;
+                float dis = Length(vec);
+                if (!(dis < 0.001f)) {
+                    C3 fr = MatFr(S, mat, Lo(it, wo), Lo(it, r.Wi), it.UV);
+                    C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
+                    W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
+                    zero = false;
+                    ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
+                    o->shadow = true;
+                }
+            }
+            if (zero) fl |= F_DZERO;
+        }
+    }
+}
+
 template <bool kAdj>
 DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, unsigned long long* stats, bool counting,
                    int pass, const WfAdjoint& A, float* s_alpha) {
@@ -497,16 +585,19 @@ DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, uns
         grad = IsValid(Ltot) && (dL.r != 0.0f || dL.g != 0.0f || dL.b != 0.0f);
     }
 
-    /* 1. the direct term scheduled by the previous bounce */
+    /* 1. the direct term scheduled by the previous bounce (or, All strategy,
+     * the term of one light of this vertex) */
+    bool resume = false;                     /* All: the vertex's last light is in, its continuation runs below */
     if (fl & F_PENDING) {
         float4 pc = W.pd_coeff[slot];
         C3 coeffb = c3(pc.x, pc.y, pc.z);
         float lightPdf = pc.w;
+        const bool all = (fl & F_ALL) != 0;
         if (P.method == RT_METHOD_MIS) {
             C3 direct = c3s(0);
             C3 tl = c3s(0.0f), tb = c3s(0.0f);
+            C3 le = c3s(0.0f);
             if (!(fl & F_DZERO)) {
-                C3 le = c3s(0.0f);
                 if ((fl & F_L1) && !W.occluded[slot]) {
                     float4 l1 = W.pd_l1[slot];
                     tl = c3(l1.x, l1.y, l1.z);
@@ -528,10 +619,17 @@ DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, uns
                     }
                     if (!IsBlack(li)) { tb = c3(fr2.x, fr2.y, fr2.z) * li * fr2.w / mi.x; le = le + tb; }
                 }
-                direct = direct + le / lightPdf;
+                if (!all) direct = direct + le / lightPdf;
             }
-            radiance = radiance + coeffb * direct;
-            if (kAdj && grad) {
+            if (all) {
+                /* PathTracer.cs:297-304: result += EstimateDirect(light) over Scene.Lights */
+                const float4 ac = W.pd_acc[slot];
+                const C3 acc = c3(ac.x, ac.y, ac.z) + le;
+                W.pd_acc[slot] = make_float4(acc.r, acc.g, acc.b, ac.w);
+            } else {
+                radiance = radiance + coeffb * direct;
+            }
+            if (kAdj && grad && !all) {
                 /* alpha terms of the pending vertex: its two direct terms, then its
                  * continuation, which carries everything after its direct light */
                 const float4 ar = W.adj_rho[slot];
@@ -546,9 +644,35 @@ DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, uns
         } else { /* NEE */
             C3 e = c3s(0);
             if (!(fl & F_DZERO) && !W.occluded[slot]) { float4 l1 = W.pd_l1[slot]; e = c3(l1.x, l1.y, l1.z); }
-            radiance = radiance + coeffb * e / lightPdf;
+            radiance = all ? radiance + coeffb * e : radiance + coeffb * e / lightPdf;
         }
         fl &= ~(F_PENDING | F_L1 | F_L2 | F_DZERO);
+        if (all) {
+            const float4 ac = W.pd_acc[slot];
+            const int next = __float_as_int(ac.w) + 1;
+            if (next < S->light_count) {
+                /* the next light at the same vertex: its draws follow the previous light's */
+                const float4 ro = W.ray_o[slot], rdd = W.ray_d[slot];
+                const Ray ray = mkray(v3(ro.x, ro.y, ro.z), v3(rdd.x, rdd.y, rdd.z), ro.w, rdd.w);
+                Isect it;
+                load_hit(S, ray, W.ext_hit[slot], W.ext_sub[slot], &it);
+                const int4 px = W.pix[slot];
+                Rng rand;
+                rng_resume(rand, P.seed, (uint32_t)(P.x0 + px.x), (uint32_t)(P.y0 + px.y), (uint32_t)px.w, W.rng_n[slot]);
+                float4 rho = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+                schedule_direct<kAdj>(o, W, S, slot, it, -ray.D, PrimOf(S, it).material, next, 1.0f, coeffb, P.method,
+                                      rand, fl, rho);
+                W.pd_acc[slot] = make_float4(ac.x, ac.y, ac.z, __int_as_float(next));
+                W.rng_n[slot] = rand.n;
+                W.flags[slot] = fl;
+                W.rad[slot] = make_float4(radiance.r, radiance.g, radiance.b, 0);
+                o->keep = true;
+                return;
+            }
+            if (P.method == RT_METHOD_MIS) radiance = radiance + coeffb * c3(ac.x, ac.y, ac.z);
+            fl &= ~F_ALL;
+            resume = true;
+        }
     }
 
     bool done = (fl & F_DONE) != 0;
@@ -565,11 +689,13 @@ DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, uns
         Ray nray = ray;
         bool ext = false;
         do {
-            if (++guard > RT_LOOP_CAP) { atomicOr(status, RT_STATUS_ITER); done = true; break; }
+            if (!resume && ++guard > RT_LOOP_CAP) { atomicOr(status, RT_STATUS_ITER); done = true; break; }
             Isect it;
             bool isHit = load_hit(S, ray, W.ext_hit[slot], W.ext_sub[slot], &it);
             V3 wo = -ray.D;
-            if (P.method == RT_METHOD_BXDF) {
+            if (resume) {
+                /* All: emission and the lights of this vertex are in; its continuation follows */
+            } else if (P.method == RT_METHOD_BXDF) {
                 if (!isHit) { radiance = radiance + coeff * EvalAllInfinite(S, ray.D); done = true; break; }
                 if (P.max_depth != -1 && bounces >= P.max_depth) { done = true; break; }
                 if (!HasSurface(S, it)) { nray = mkray(it.P, ray.D, ray.MinT); ext = true; break; }
@@ -595,84 +721,19 @@ DF void shade_path(PathOut* o, const WfState& W, int slot, uint32_t* status, uns
                     }
                     if (A.alpha_slot) rho.w = __int_as_float(A.alpha_slot[mat]);
                 }
-                int light;
-                float lightPdf = SampleLight(S, rand, &light);
-                if (P.method == RT_METHOD_MIS) {
-                    fl |= F_PENDING;
-                    W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
-                    if (lightPdf > 0.0f) {
-                        V3 wod = it.Wr;
-                        LSample ls = LightSampleLi(S, light, it.P, rand);
-                        if (ls.Pdf > 0.0f && !IsBlack(ls.Li)) {
-                            C3 fr = MatFr(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
-                            float scatteringPdf = MatPdf(S, mat, Lo(it, wod), Lo(it, ls.Wi), it.UV);
-                            if (!IsBlack(fr)) {
-                                /* IsOccluded(it.P, ls.P) */
-                                V3 vec = ls.P - it.P;
-                                float dis = Length(vec);
-                                if (!(dis < 0.001f)) {
-                                    fr = fr * AbsCosTheta(Lo(it, ls.Wi));
-                                    float weight = PowerHeuristic(ls.Pdf, scatteringPdf);
-                                    if (kAdj && __float_as_int(rho.w) >= 0)
-                                        rho.x = DirectDln(S, mat, Lo(it, wod), Lo(it, ls.Wi), weight, true, it.UV);
-                                    C3 l1 = fr * ls.Li * weight / ls.Pdf;
-                                    W.pd_l1[slot] = make_float4(l1.r, l1.g, l1.b, 0);
-                                    fl |= F_L1;
-                                    ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
-                                    o->shadow = true;
-                                }
-                            }
-                        }
-                        BSample sample = MatSample(S, mat, Lo(it, wod), it.UV, rand);
-                        C3 fr = sample.Fr * AbsCosTheta(sample.Wi);
-                        float scatteringPdf = sample.Pdf;
-                        bool sampledSpecular = (sample.Type & BX_SPECULAR) != 0;
-                        if (!IsBlack(fr) && scatteringPdf > 0) {
-                            float weight = 1;
-                            bool go = true;
-                            if (!sampledSpecular) {
-                                float bxdfToLightPdf = LightPdfLi(S, light, it.P, Wo(it, sample.Wi));
-                                if (bxdfToLightPdf == 0.0f) go = false;
-                                else weight = PowerHeuristic(scatteringPdf, bxdfToLightPdf);
-                            }
-                            if (go) {
-                                if (kAdj && __float_as_int(rho.w) >= 0)
-                                    rho.y = DirectDln(S, mat, Lo(it, wod), sample.Wi, sampledSpecular ? 2.0f : weight, false,
-                                                      it.UV);
-                                Ray toLight = Spawn(it, Wo(it, sample.Wi));
-                                V3 wle = Wo(it, -sample.Wi);
-                                W.pd_fr[slot] = make_float4(fr.r, fr.g, fr.b, weight);
-                                W.pd_mis[slot] = make_float4(scatteringPdf, __int_as_float(light), 0, 0);
-                                W.pd_w[slot] = make_float4(wle.x, wle.y, wle.z, 0);
-                                W.pd_ray_o[slot] = make_float4(toLight.O.x, toLight.O.y, toLight.O.z, toLight.MinT);
-                                W.pd_ray_d[slot] = make_float4(toLight.D.x, toLight.D.y, toLight.D.z, toLight.MaxT);
-                                fl |= F_L2;
-                                o->mis = true;
-                            }
-                        }
-                    } else {
-                        fl |= F_DZERO;
+                if (P.strategy == RT_STRATEGY_ALL) {
+                    if (S->light_count > 0) {
+                        /* light 0 now, the others one per iteration; the continuation waits */
+                        fl |= F_ALL;
+                        W.pd_acc[slot] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0));
+                        schedule_direct<kAdj>(o, W, S, slot, it, wo, mat, 0, 1.0f, coeff, P.method, rand, fl, rho);
+                        break;
                     }
-                } else { /* NEE: NeeEstimateLight */
-                    if (lightPdf > 0.0f) {
-                        fl |= F_PENDING;
-                        W.pd_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, lightPdf);
-                        LSample r = LightSampleLi(S, light, it.P, rand);
-                        bool zero = true;
-                        if (r.Pdf > 0.0f) {
-                            V3 vec = r.P - it.P;
-                            float dis = Length(vec);
-                            if (!(dis < 0.001f)) {
-                                C3 fr = MatFr(S, mat, Lo(it, wo), Lo(it, r.Wi), it.UV);
-                                C3 e = fr * r.Li * AbsCosTheta(Lo(it, r.Wi)) / r.Pdf;
-                                W.pd_l1[slot] = make_float4(e.r, e.g, e.b, 0);
-                                zero = false;
-                                ray4(mkray(it.P, Normalize(vec), 0.0001f, dis - 0.0001f), &o->so, &o->sd);
-                                o->shadow = true;
-                            }
-                        }
-                        if (zero) fl |= F_DZERO;
-                    }
+                    if (P.method == RT_METHOD_MIS) radiance = radiance + coeff * c3s(0.0f);
+                } else {
+                    int light;
+                    float lightPdf = SampleLight(S, rand, &light);
+                    schedule_direct<kAdj>(o, W, S, slot, it, wo, mat, light, lightPdf, coeff, P.method, rand, fl, rho);
                 }
                 if (kAdj) W.adj_rho[slot] = rho;
             }

@@ -101,6 +101,7 @@ struct WfState {
     float4* pd_mis;          /* BSDF pdf, light index */
     float4* pd_w;            /* direction passed to the light's L() */
     float4* pd_ray_o; float4* pd_ray_d;
+    float4* pd_acc;          /* All light strategy: the vertex's summed direct terms, light index (int bits) */
     /* ray results */
     float4* ext_hit; int32_t* ext_sub;
     float4* mis_hit; int32_t* mis_sub;

@@ -132,6 +132,22 @@ def test_batch_of_volumes_matches_single_renders():
             d.close()
 
 
+def test_batch_all_light_strategy(scenes):
+    """`path` items with the All light strategy (every light estimated at each
+    vertex, one light per wavefront iteration) reproduce their single renders,
+    Uniform items alongside them too."""
+    (a, sa), (b, sb), _ = scenes
+    host = Device(0)
+    try:
+        items = [(a, sa.replace(spp=2, strategy=N.STRATEGY_ALL)), (b, sb.replace(spp=2)),
+                 (b, sb.replace(spp=1, seed=9, strategy=N.STRATEGY_ALL))]
+        films = host.render_batch(items)
+        for (d, st), f in zip(items, films):
+            assert np.array_equal(_bits(f), _bits(d.render(st)))
+    finally:
+        host.close()
+
+
 def test_batch_rejects_unsupported_items(scenes):
     (a, sa), (b, sb), _ = scenes
     host = Device(0)
@@ -140,7 +156,7 @@ def test_batch_rejects_unsupported_items(scenes):
             host.render_batch([(a, sa.replace(spp=1)), (b, sb.replace(spp=1, integrator=N.INTEGRATOR_VOL_PATH))])
         assert e.value.code == N.RT_ERR_UNSUPPORTED
         with pytest.raises(N.RTError) as e:
-            host.render_batch([(a, sa.replace(spp=1, strategy=N.STRATEGY_ALL))])
+            host.render_batch([(a, sa.replace(spp=1, integrator=N.INTEGRATOR_VOL_PATH, strategy=N.STRATEGY_ALL))])
         assert e.value.code == N.RT_ERR_UNSUPPORTED
         with pytest.raises(N.RTError) as e:
             host.render_batch([(a, sa.replace(spp=1))] * (N.MAX_BATCH + 1))

@@ -50,7 +50,7 @@ def test_films_golden(dev, case):
     want = _load("film_" + name)["film"]
     dev.upload(scene)
     modes = [N.RENDERER_MEGAKERNEL]
-    if st.strategy == N.STRATEGY_UNIFORM:
+    if st.strategy == N.STRATEGY_UNIFORM or st.integrator == N.INTEGRATOR_PATH:
         modes += [N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH]
     try:
         for m in modes:

@@ -133,8 +133,6 @@ def _render(dev, st, renderer):
 @pytest.mark.parametrize("strategy", [N.STRATEGY_UNIFORM, N.STRATEGY_ALL])
 def test_render_cornell_bitexact(dev, cornell, method, strategy, renderer):
     s, st, orc = cornell
-    if renderer in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) and strategy == N.STRATEGY_ALL:
-        pytest.skip("the wavefront renderer runs the Uniform light strategy")
     dev.upload(s)
     st = st.replace(spp=3, method=method, strategy=strategy)
     g, o = _render(dev, st, renderer), orc.render(st)
@@ -244,3 +242,42 @@ def test_counters_match_oracle(dev, cornell, renderer):
     _, o = orc.render(st, stats=True)
     for k in ("samples", "rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
         assert g[k] == o[k], (k, g[k], o[k])
+
+
+@pytest.mark.parametrize("renderer", [N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH])
+@pytest.mark.parametrize("method", [N.METHOD_MIS, N.METHOD_NEE])
+def test_all_light_strategy_on_the_wavefront(dev, zoo, method, renderer):
+    """The All light strategy (PathTracer.cs:297-304) on the wavefront: every light
+    of a vertex - the zoo's two quad triangles, its sphere emitter and its
+    environment - is estimated in the reference's order, one light per
+    iteration, before the continuation; films bit for bit and ray counts equal
+    to the oracle's."""
+    s, st, orc = zoo
+    dev.upload(s)
+    st = st.replace(method=method, strategy=N.STRATEGY_ALL, spp=2)
+    dev.set_counting(True)
+    try:
+        g = _render(dev, st, renderer)
+        gc = dev.stats()
+    finally:
+        dev.set_counting(False)
+    o, oc = orc.render(st, stats=True)
+    assert np.array_equal(_bits(g), _bits(o)), f"max abs diff {np.abs(g - o).max()}"
+    if renderer == N.RENDERER_WAVEFRONT:
+        for k in ("samples", "rays_closest", "rays_shadow", "node_visits", "prim_tests", "instance_visits"):
+            assert gc[k] == oc[k], (k, gc[k], oc[k])
+
+
+def test_vol_path_all_strategy_stays_on_the_megakernel(dev):
+    s, st = procedural.volume_box(16, 16)
+    dev.upload(s)
+    st = st.replace(strategy=N.STRATEGY_ALL, spp=1)
+    try:
+        dev.set_renderer(N.RENDERER_WAVEFRONT)
+        with pytest.raises(N.RTError) as e:
+            dev.render(st)
+        assert e.value.code == N.RT_ERR_UNSUPPORTED
+        dev.set_renderer(N.RENDERER_AUTO)            # AUTO picks the megakernel
+        assert np.array_equal(_bits(dev.render(st)), _bits(OracleScene(s).render(st)))
+    finally:
+        dev.set_renderer(N.RENDERER_AUTO)
