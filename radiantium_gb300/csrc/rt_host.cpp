@@ -195,7 +195,7 @@ void ensure_wf(Ctx* c, int slots) {
     const size_t n = (size_t)slots, q = 3 * (size_t)slots;
     W.q_o = wf_alloc<float4>(c, q); W.q_d = wf_alloc<float4>(c, q); W.q_meta = wf_alloc<int32_t>(c, q);
     W.active[0] = wf_alloc<int32_t>(c, n); W.active[1] = wf_alloc<int32_t>(c, n);
-    W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint8_t>(c, n);
+    W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint8_t>(c, n); W.mark = wf_alloc<uint8_t>(c, n);
     W.job = wf_alloc<uint8_t>(c, n);
     W.pix = wf_alloc<int4>(c, n); W.rng_n = wf_alloc<uint32_t>(c, n);
     W.coeff = wf_alloc<float4>(c, n); W.rad = wf_alloc<float4>(c, n);
@@ -970,6 +970,7 @@ void particle_wavefront(Ctx* c, const RtParams& P, int64_t first, int64_t count,
     W.shadow_base = 2 * slots;
     W.refill = c->wf_refill;
     W.iter_cap = c->wf_iter_cap;
+    W.dense_sort = 1;
     WfMode m;
     m.particle = true;
     m.sort = c->mat_types > 1;
@@ -1262,6 +1263,8 @@ void wavefront_run(Ctx* c, const std::vector<WfJobIn>& jobs, cudaStream_t s, boo
         W.shadow_base = 2 * slots;
         W.refill = c->wf_refill;
         W.iter_cap = c->wf_iter_cap;
+        /* vol_path's shade runs slower from slots walked in index order (C3: 115.3 -> 112.5 M samples/s) */
+        W.dense_sort = mode.vol ? 0 : 1;
         /* one pass over the round's samples: start every slot, bounce until no path is left */
         auto run_pass = [&](int pass) {
             wf_round(c, W, s, use_graph, mode, pass, adj, total, (int)act.size(), &tot);

@@ -133,6 +133,11 @@ DF bool in_bounds(const WfState&, long long, long long) { return true; }
 #endif
 DF void set_active(const WfState& W, int list, int a, int slot) {
     if (in_bounds(W, a, W.slots)) W.active[list][a] = slot;
+    if (in_bounds(W, slot, W.slots)) W.mark[slot] = (uint8_t)(list + 1);
+}
+/* a shaded slot that leaves the active lists */
+DF void clear_active(const WfState& W, int slot) {
+    if (slot >= 0 && in_bounds(W, slot, W.slots)) W.mark[slot] = 0;
 }
 
 DF void push_ray4(const WfState& W, int q, int path, int kind, float4 o, float4 d) {
@@ -798,6 +803,7 @@ DF void path_queues(const WfState& W, int slot, int next, PathOut& o) {
         push_ray4(W, qe, slot, WF_RAY_EXT, ro, rd);
     }
     if (o.keep) set_active(W, next, qa, slot);
+    else clear_active(W, slot);
 }
 
 /* ---- vol_path (VolumetricPathTracer.Li, Integrators/VolumetricPathTracer.cs) ----
@@ -1173,6 +1179,7 @@ DF void vol_queues(const WfState& W, int slot, int next, VolOut& o) {
         push_ray4(W, qe, slot, WF_RAY_EXT, ro, rd);
     }
     if (o.keep) set_active(W, next, qa, slot);
+    else clear_active(W, slot);
 }
 
 __global__ void __launch_bounds__(128, RT_VSHADE_BLOCKS) k_wf_shade_vol(WfState W, uint32_t* status, unsigned long long* stats,
@@ -1322,6 +1329,7 @@ DF void particle_queues(const WfState& W, int slot, int next, const PartOut& o) 
     if (o.splat) push_ray4(W, qs, slot, WF_RAY_SPLAT, o.so, o.sd);
     if (o.ext) push_ray4(W, qe, slot, WF_RAY_EXT, o.eo, o.ed);
     if (o.keep) set_active(W, next, a, slot);
+    else clear_active(W, slot);
 }
 
 __global__ void __launch_bounds__(256) k_wf_start_particles(WfState W) {
@@ -1439,6 +1447,7 @@ __global__ void k_wf_active_init(WfState W) {
     bool alive = (W.flags[i] & F_ALIVE) != 0;
     int a = warp_append(&W.ctr->n_active[0], alive);
     if (alive) set_active(W, 0, a, i);
+    else W.mark[i] = 0;
 }
 
 /* Code key of an active path: which code the shade kernel will run for it.
@@ -1471,15 +1480,36 @@ __global__ void k_wf_phase(WfState W) {
     for (int k = threadIdx.x; k < 2 * WF_SHADE_KEYS; k += blockDim.x) W.ctr->key_count[k] = 0;
 }
 
+/* The sort's input order.  While at least one slot in WF_DENSE_SORT is active
+ * (and the run allows it: W.dense_sort),
+ * the sort walks the slots in index order (their marks say which are on this
+ * iteration's list): a warp's entries of one key then land together in slot
+ * order, so the shade's warps read path state of nearby slots - fewer sectors
+ * per field than the appended list's scattered order.  Below that it walks the
+ * active list itself.  Both kernels take the same decision from the same count. */
+#ifndef WF_DENSE_SORT
+#define WF_DENSE_SORT 8
+#endif
+DF bool sort_dense(const WfState& W, int n) { return W.dense_sort && n * WF_DENSE_SORT >= W.slots; }
+DF int sort_span(const WfState& W, int n) { return sort_dense(W, n) ? W.slots : n; }
+/* entry i of the sort's input: a slot, or -1 (a slot not on the list) */
+DF int sort_input(const WfState& W, int cur, int n, int i) {
+    if (!sort_dense(W, n)) return W.active[cur][i];
+    return W.mark[i] == cur + 1 ? i : -1;
+}
+
 /* both sort kernels are grid-stride loops: one pass with a grid sized to the
  * active count, several with a resident grid inside a graph */
 __global__ void __launch_bounds__(256) k_wf_sort_count(WfState W) {
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
-    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int span = sort_span(W, n);
+    for (int i0 = blockIdx.x * blockDim.x; i0 < span; i0 += gridDim.x * blockDim.x) {
         const int i = i0 + threadIdx.x;
-        if (i >= n) break;
-        const int key = shade_key(W, W.active[cur][i]);
+        if (i >= span) break;
+        const int slot = sort_input(W, cur, n, i);
+        if (slot < 0) continue;
+        const int key = shade_key(W, slot);
         W.sort_key[i] = (uint8_t)key;
         const unsigned peers = __match_any_sync(__activemask(), key);
         if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.ctr->key_count + key, __popc(peers));
@@ -1494,7 +1524,8 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
     __shared__ int base[WF_SHADE_KEYS];
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
-    if ((int)(blockIdx.x * blockDim.x) >= n) return;
+    const int span = sort_span(W, n);
+    if ((int)(blockIdx.x * blockDim.x) >= span) return;
     const int t = threadIdx.x;
     int v = W.ctr->key_count[t];
     base[t] = v;
@@ -1508,9 +1539,11 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
     base[t] -= v;                                           /* exclusive */
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
-    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    for (int i0 = blockIdx.x * blockDim.x; i0 < span; i0 += gridDim.x * blockDim.x) {
         const int i = i0 + threadIdx.x;
-        if (i >= n) break;
+        if (i >= span) break;
+        const int slot = sort_input(W, cur, n, i);
+        if (slot < 0) continue;
         const int key = W.sort_key[i];
         const unsigned peers = __match_any_sync(__activemask(), key);
         const int leader = __ffs(peers) - 1;
@@ -1518,7 +1551,7 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
         if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
         first = __shfl_sync(peers, first, leader);
         const int dst = base[key] + first + __popc(peers & ((1u << lane) - 1u));
-        if (in_bounds(W, dst, W.slots)) W.sorted[dst] = W.active[cur][i];
+        if (in_bounds(W, dst, W.slots)) W.sorted[dst] = slot;
     }
 }
 

@@ -80,11 +80,13 @@ struct WfState {
     uint32_t* status;        /* the context's status word (RT_STATUS_*) */
     int32_t refill;          /* idle lanes of a trace warp before it fetches new rays */
     int32_t iter_cap;        /* bounce iterations of one round before the run gives up (WF_ITER_CAP) */
+    int32_t dense_sort;      /* the shade-key sort may walk the slots in index order (not for vol_path) */
     WfCounters* ctr;
     const WfJob* jobs;
     /* active slot lists by iteration parity, and the list regrouped by shade key */
     int32_t* active[2];
     int32_t* sorted; uint8_t* sort_key;
+    uint8_t* mark;           /* per slot: 1 + the active list (iteration parity) it is on, 0 if none */
     /* path state */
     uint8_t* job;            /* job of the slot's path */
     int4* pix;               /* crop x, crop y, sample index in chunk, sample index t */
