@@ -7,8 +7,12 @@
  *
  * Parity status: the reference is C#/.NET 6 and cannot run on this machine
  * (no dotnet/mono) and ships no tests or golden vectors, so this restatement
- * is "parity unpinned" against the reference binary; it is pinned against
- * analytic known answers and against the GPU library bit for bit.
+ * cannot be compared with the reference binary's outputs.  It is pinned by
+ * the reference's own example scenes (tests/fixtures/reference: the scene
+ * files load into the primitive list and Scene.Lights RendererBuilder.Build
+ * makes, and render on the GPU library bit for bit like here), by analytic
+ * known answers, and by the GPU library, bit for bit, up to the benchmark
+ * sizes.
  *
  * Every operation keeps the reference's expression order; compile with
  * -ffp-contract=off so no multiply-add is fused (the C# JIT never fuses).
