@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--renderer", choices=["auto", "megakernel", "wavefront", "graph"], default="auto")
     ap.add_argument("--traversal", choices=["exact", "wide"], default="exact",
                     help="exact: the reference's tree and order (bit-exact films); wide: the opt-in fast traversal")
+    ap.add_argument("--light-sampling", choices=["cdf", "alias"], default="cdf",
+                    help="cdf: the reference's CDF search (bit-exact films); alias: opt-in alias tables (same pmf)")
     ap.add_argument("--no-fd-check", action="store_true", help="adjoint workload: skip the finite-difference check")
     ap.add_argument("--no-relmse", action="store_true", help="skip the converged render for relMSE")
     ap.add_argument("--no-subrecords", action="store_true",
@@ -309,6 +311,7 @@ def run_ours(args):
             "graph": N.RENDERER_WAVEFRONT_GRAPH}[args.renderer]
     dev.set_renderer(mode)
     traversal = N.TRAVERSAL_WIDE if args.traversal == "wide" else N.TRAVERSAL_EXACT
+    light_sampling = N.LIGHT_SAMPLING_ALIAS if args.light_sampling == "alias" else N.LIGHT_SAMPLING_CDF
     uses_wavefront = mode in (N.RENDERER_WAVEFRONT, N.RENDERER_WAVEFRONT_GRAPH) or (
         mode == N.RENDERER_AUTO and st.strategy == N.STRATEGY_UNIFORM)
     upload_s = time.perf_counter() - t0
@@ -338,6 +341,7 @@ def run_ours(args):
     dev.set_counting(False)
 
     dev.set_traversal(traversal)            # the counting pass above ran the exact traversal
+    dev.set_light_sampling(light_sampling)
     for i in range(args.warmup):
         dev.render_device(st.replace(spp=spp_step, sample_begin=base + i * spp_step), film.data_ptr(), stream)
     torch.cuda.synchronize()
@@ -414,9 +418,15 @@ def run_ours(args):
                        "call copies (rt_stats.h2d_bytes)"}
 
     # the opt-in wide traversal on the same passes (the headline stays on the exact one)
-    wide = None
-    if uses_wavefront and traversal == N.TRAVERSAL_EXACT and not args.no_subrecords and rank == 0:
-        wide = wide_subrecord(dev, st, spp_step, base + args.warmup * spp_step, film, flush, stream, value, ms_step)
+    wide = alias = both = None
+    if uses_wavefront and traversal == N.TRAVERSAL_EXACT and light_sampling == N.LIGHT_SAMPLING_CDF \
+            and not args.no_subrecords and rank == 0:
+        sub = lambda t, l: mode_subrecord(dev, st, spp_step, base + args.warmup * spp_step, film, flush, stream,
+                                          value, ms_step, t, l)
+        wide = sub(N.TRAVERSAL_WIDE, N.LIGHT_SAMPLING_CDF)
+        if any(g.kind == N.GROUP_INFINITE_LIGHT for g in scene.groups):
+            alias = sub(N.TRAVERSAL_EXACT, N.LIGHT_SAMPLING_ALIAS)
+            both = sub(N.TRAVERSAL_WIDE, N.LIGHT_SAMPLING_ALIAS)
 
     # the plain megakernel on the same passes, for the wavefront / megakernel ratio
     plain = None
@@ -478,7 +488,10 @@ def run_ours(args):
                 "autotune": tuned,
                 "traversal": ("exact (the reference's tree and visit order)" if traversal == N.TRAVERSAL_EXACT
                               else "wide (opt-in fast traversal; the counting pass and algorithmic bytes use "
-                                   "the exact one)")},
+                                   "the exact one)"),
+                "light_sampling": ("cdf (the reference's CDF search)" if light_sampling == N.LIGHT_SAMPLING_CDF
+                                   else "alias (opt-in alias tables, the same texel pmf; the counting pass uses "
+                                        "the CDF search)")},
         "mrays_per_s": (counts["rays_closest"] + counts["rays_shadow"]) * world / (ms_step / 1000.0) / 1e6,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src,
@@ -491,6 +504,8 @@ def run_ours(args):
                                         "k_wf_trace_closest)") if l2f is not None else None},
         "plain_megakernel": plain,
         "wide_traversal": wide,
+        "alias_light_sampling": alias,
+        "wide_traversal_and_alias_light_sampling": both,
         "relmse": relmse,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -511,17 +526,22 @@ def run_ours(args):
     return 0
 
 
-def wide_subrecord(dev, st, spp_step, begin, film, flush, stream, exact_value, exact_ms, steps=4, warmup=2):
-    """The same passes with the opt-in wide traversal (RT_TRAVERSAL_WIDE): its
-    samples/s against the exact traversal's, and how far one pass's film is
-    from the exact film (share of identical floats, relative mean squared
-    difference)."""
+def mode_subrecord(dev, st, spp_step, begin, film, flush, stream, exact_value, exact_ms, traversal, light_sampling,
+                   steps=4, warmup=2):
+    """The same passes with opt-in modes: the wide traversal (RT_TRAVERSAL_WIDE)
+    and / or alias-table environment sampling (RT_LIGHT_SAMPLING_ALIAS).  Their
+    samples/s against the default modes'; for the wide traversal alone, how far
+    one pass's film is from the exact film (share of identical floats, relative
+    mean squared difference) - alias sampling maps uniforms to other texels, so
+    its films agree only statistically (tests/test_gpu_alias.py)."""
     import torch
     from radiantium_gb300 import native as N
-    dev.set_traversal(N.TRAVERSAL_WIDE)
-    if dev.traversal() != N.TRAVERSAL_WIDE:
+    wide = traversal == N.TRAVERSAL_WIDE
+    dev.set_traversal(traversal)
+    if dev.traversal() != traversal:
         dev.set_traversal(N.TRAVERSAL_EXACT)
         return {"available": False, "note": "the scene's wide trees could overflow the traversal stack"}
+    dev.set_light_sampling(light_sampling)
     try:
         for i in range(warmup):
             dev.render_device(st.replace(spp=spp_step, sample_begin=begin + i * spp_step), film.data_ptr(), stream)
@@ -537,20 +557,30 @@ def wide_subrecord(dev, st, spp_step, begin, film, flush, stream, exact_value, e
             times.append(e0.elapsed_time(e1))
             trace += dev.stats()["render_kernel_ms"]
         ms = float(np.mean(times))
-        wide_film = film.clone()
+        mode_film = film.clone()
     finally:
         dev.set_traversal(N.TRAVERSAL_EXACT)
-    dev.render_device(st.replace(spp=spp_step, sample_begin=begin + (steps - 1) * spp_step), film.data_ptr(), stream)
-    torch.cuda.synchronize()
-    a, b = film.double(), wide_film.double()
+        dev.set_light_sampling(N.LIGHT_SAMPLING_CDF)
     value = exact_value * exact_ms / ms
-    return {"available": True, "value": value, "unit": "samples/s", "steps": steps, "ms_per_step": ms,
-            "trace_ms_per_step": trace / steps, "vs_exact": value / exact_value,
-            "identical_floats": float((film.view(torch.int32) == wide_film.view(torch.int32)).double().mean().item()),
-            "relmse_vs_exact": float((((b - a) ** 2) / (a ** 2 + 1e-2)).mean().item()),
-            "note": "rt_set_traversal(RT_TRAVERSAL_WIDE): the same trees collapsed 8-wide with quantised child boxes; "
-                    "hits equal the exact traversal's up to ties within 4 ulp and rounding-scale box culls of the "
-                    "reference (tests/test_gpu_wide_traversal.py)"}
+    out = {"available": True, "value": value, "unit": "samples/s", "steps": steps, "ms_per_step": ms,
+           "trace_ms_per_step": trace / steps, "vs_default": value / exact_value}
+    notes = []
+    if wide:
+        notes.append("rt_set_traversal(RT_TRAVERSAL_WIDE): the same trees collapsed 8-wide with quantised child "
+                     "boxes; hits equal the exact traversal's up to ties within 4 ulp and rounding-scale box culls "
+                     "of the reference (tests/test_gpu_wide_traversal.py)")
+    if light_sampling == N.LIGHT_SAMPLING_ALIAS:
+        notes.append("rt_set_light_sampling(RT_LIGHT_SAMPLING_ALIAS): O(1) alias picks with exactly the CDF "
+                     "search's texel pmf over the 2^24 uniforms (tests/test_cpu_alias.py, tests/test_gpu_alias.py)")
+    if wide and light_sampling == N.LIGHT_SAMPLING_CDF:
+        dev.render_device(st.replace(spp=spp_step, sample_begin=begin + (steps - 1) * spp_step), film.data_ptr(),
+                          stream)
+        torch.cuda.synchronize()
+        a, b = film.double(), mode_film.double()
+        out["identical_floats"] = float((film.view(torch.int32) == mode_film.view(torch.int32)).double().mean().item())
+        out["relmse_vs_exact"] = float((((b - a) ** 2) / (a ** 2 + 1e-2)).mean().item())
+    out["note"] = "; ".join(notes)
+    return out
 
 
 def batch_subrecord(args, rank, world, local, dist):

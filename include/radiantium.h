@@ -379,6 +379,26 @@ int rt_set_renderer(void* ctx, int mode);
 int rt_set_traversal(void* ctx, int mode);
 int rt_get_traversal(void* ctx, int* effective);
 
+/* ---- environment-light sampling (no counterpart in the reference) ----------
+ * How an infinite light's Distribution2D (Distribution2D.cs:9-61) picks a
+ * texel in SampleLi and SampleEmit (Lights/InfiniteAreaLight.cs:92-133).
+ * RT_LIGHT_SAMPLING_CDF (default): the reference's binary search over the
+ * marginal and conditional CDFs (Distribution1D.cs:51-85); films equal the
+ * reference's restatement bit for bit.
+ * RT_LIGHT_SAMPLING_ALIAS: an opt-in O(1) alias-table pick from the same two
+ * uniforms.  Over the renderer's uniforms (k / 2^24) it draws every texel for
+ * exactly as many values of k as the CDF search does, so both modes sample
+ * the same texel pmf and report the same pdf; only which uniform maps to
+ * which texel differs, so films agree statistically, not bit for bit.  A light
+ * whose table is not a non-decreasing CDF (negative or non-finite texels)
+ * keeps the search.  The mode belongs to the context's scene: it applies to
+ * every render of that scene, in a batch too, and may be set before or after
+ * rt_upload_scene (not while a call on the context is running). */
+#define RT_LIGHT_SAMPLING_CDF 0
+#define RT_LIGHT_SAMPLING_ALIAS 1
+int rt_set_light_sampling(void* ctx, int mode);
+int rt_get_light_sampling(void* ctx, int* mode);
+
 /* One render of a batch: the context holding its uploaded scene (may be the
  * batch context itself), its parameters and its host output film (crop,
  * ColorBuffer layout, width * height * 3 floats). */

@@ -109,6 +109,7 @@ struct Ctx {
     std::vector<cudaEvent_t> events;           /* per-launch timing of the path-tracing kernel */
     int renderer = RT_RENDERER_AUTO;
     int traversal = RT_TRAVERSAL_EXACT;        /* rt_set_traversal */
+    int light_sampling = RT_LIGHT_SAMPLING_CDF; /* rt_set_light_sampling */
     int wf_iter_cap = WF_ITER_CAP;             /* bounce iterations of one wavefront round (test hook) */
     /* wavefront path state */
     WfState wf{};
@@ -289,6 +290,56 @@ void dist1d(std::vector<float>& pool, const float* f, int n, int64_t* pdf_off, i
     else { for (int i = 1; i < n + 1; i++) cdf[i] /= in; }
     pool.insert(pool.end(), cdf.begin(), cdf.end());
     *integ = in;
+}
+
+/* Walker's alias table for the pmf that the CDF search of a Distribution1D
+ * (Distribution1D.cs:51-85) samples on the renderer's uniforms u = k / 2^24,
+ * k in [0, 2^24).  FindInterval picks entry i for exactly
+ *     c_i = ceil(cdf[i+1] 2^24) - ceil(cdf[i] 2^24)
+ * values of k.  The alias pick (AliasPick, rt_shading.cuh) sends k to bucket
+ * i = floor(k n / 2^24), which holds the B_i = ceil((i+1) 2^24 / n) -
+ * ceil(i 2^24 / n) values of k from k0_i = ceil(i 2^24 / n) up, in increasing
+ * order of rem = k n - i 2^24; it keeps i for the first own_i of them (rem <
+ * threshold_i = (k0_i + own_i) n - i 2^24) and hands the rest to alias_i.
+ * Vose's pairing, run on these integer counts, makes own_i plus what the other
+ * buckets hand to i equal c_i for every i, so the alias pick and the search
+ * draw every entry for the same number of k: the same pmf, exactly.  (A
+ * bucket short of B_i takes the rest from one with more; buckets differ in
+ * size by at most one, so a donor never goes below zero.)  Appends n
+ * {threshold, alias} pairs; returns false, appending nothing, when the table is
+ * not a non-decreasing CDF from 0 to 1 (negative or non-finite inputs). */
+bool alias_from_cdf(const float* cdf, int n, std::vector<int2>& out) {
+    const int64_t K = int64_t(1) << 24;
+    if (n <= 0 || n > (1 << 24) || !(cdf[0] == 0.0f) || !(cdf[n] == 1.0f)) return false;
+    auto kceil = [](float x) { return (int64_t)std::ceil((double)x * 16777216.0); };
+    std::vector<int64_t> c(n), B(n), k0(n + 1);
+    for (int i = 0; i <= n; i++) k0[i] = ((int64_t)i * K + n - 1) / n;
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(cdf[i + 1]) || cdf[i + 1] < cdf[i]) return false;
+        c[i] = kceil(cdf[i + 1]) - kceil(cdf[i]);
+        B[i] = k0[i + 1] - k0[i];
+    }
+    std::vector<int> alias(n), small, large;
+    for (int i = 0; i < n; i++) {
+        alias[i] = i;
+        if (c[i] < B[i]) small.push_back(i);
+        else if (c[i] > B[i]) large.push_back(i);
+    }
+    while (!small.empty()) {
+        const int s = small.back();
+        small.pop_back();
+        if (large.empty()) return false;   /* unreachable: deficits and surpluses both sum to the same */
+        const int l = large.back();
+        alias[s] = l;
+        c[l] -= B[s] - c[s];
+        if (c[l] <= B[l]) {
+            large.pop_back();
+            if (c[l] < B[l]) small.push_back(l);
+        }
+    }
+    for (int i = 0; i < n; i++)
+        out.push_back(make_int2((int32_t)((k0[i] + c[i]) * n - (int64_t)i * K), alias[i]));
+    return true;
 }
 
 struct TopPrim {
@@ -613,6 +664,7 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
      * world sphere from the top-level bounds (Light.cs:181-187) */
     std::vector<RtDist2D> dists;
     std::vector<float> pool;
+    std::vector<int2> alias;
     const rtb::Box& wb = top.nodes[0].bounds;
     for (int li : infinite) {
         RtLight& L = lights[li];
@@ -650,6 +702,13 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
         D.cond_int = (int64_t)pool.size();
         pool.insert(pool.end(), cond_int.begin(), cond_int.end());
         dist1d(pool, cond_int.data(), H, &D.marg_pdf, &D.marg_cdf, &D.marg_int);
+        {   /* the alias tables of the same CDFs (RT_LIGHT_SAMPLING_ALIAS) */
+            const size_t at = alias.size();
+            bool ok = alias_from_cdf(pool.data() + D.marg_cdf, H, alias);
+            for (int y = 0; ok && y < H; y++) ok = alias_from_cdf(pool.data() + D.cond_cdf + (int64_t)y * (W + 1), W, alias);
+            if (ok) { D.marg_alias = (int64_t)at; D.cond_alias = (int64_t)at + H; }
+            else { alias.resize(at); D.marg_alias = D.cond_alias = -1; }
+        }
         L.dist = (int)dists.size();
         dists.push_back(D);
         float cx = (wb.mx[0] + wb.mn[0]) * 0.5f, cy = (wb.mx[1] + wb.mn[1]) * 0.5f, cz = (wb.mx[2] + wb.mn[2]) * 0.5f;
@@ -707,6 +766,8 @@ void upload_scene(Ctx* c, const rt_scene_desc* d) {
     v.infinite_lights = upload(c, infinite);
     v.dists = upload(c, dists);
     v.dist_pool = upload(c, pool);
+    v.alias_pool = upload(c, alias);
+    v.env_alias = c->light_sampling == RT_LIGHT_SAMPLING_ALIAS ? 1 : 0;
     v.light_count = (int)lights.size();
     v.infinite_count = (int)infinite.size();
     v.global_medium = d->global_medium < 0 ? -1 : d->global_medium;
@@ -1727,6 +1788,24 @@ int rt_set_traversal(void* ctx, int mode) {
     c->traversal = mode;
     return RT_OK;
 }
+int rt_set_light_sampling(void* ctx, int mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || (mode != RT_LIGHT_SAMPLING_CDF && mode != RT_LIGHT_SAMPLING_ALIAS)) return RT_ERR_INVALID_ARG;
+    return run(c, [&] {
+        c->light_sampling = mode;
+        if (!c->has_scene) return;
+        /* the flag lives in the scene's device view, which every kernel reads */
+        c->view.env_alias = mode == RT_LIGHT_SAMPLING_ALIAS ? 1 : 0;
+        CK(cudaMemcpyAsync(c->d_view, &c->view, sizeof(RtSceneView), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+int rt_get_light_sampling(void* ctx, int* mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !mode) return RT_ERR_INVALID_ARG;
+    *mode = c->light_sampling;
+    return RT_OK;
+}
 int rt_get_traversal(void* ctx, int* effective) {
     Ctx* c = (Ctx*)ctx;
     if (!c || !effective) return RT_ERR_INVALID_ARG;
@@ -1857,6 +1936,45 @@ int rt_debug_set_gpu_build(void* ctx, int min_prims) {
     if (!c || min_prims < 0) return RT_ERR_INVALID_ARG;
     c->gpu_build_min = min_prims == 0 ? INT_MAX : min_prims;
     return RT_OK;
+}
+
+/* test hook (not part of radiantium.h): the alias table alias_from_cdf builds
+ * for a CDF of n + 1 floats, as n {threshold, alias} pairs; no CUDA call */
+int rt_debug_alias(const float* cdf, int n, int32_t* out) {
+    if (!cdf || !out || n <= 0) return RT_ERR_INVALID_ARG;
+    try {
+        std::vector<int2> t;
+        if (!alias_from_cdf(cdf, n, t)) return RT_ERR_UNSUPPORTED;
+        std::memcpy(out, t.data(), t.size() * sizeof(int2));
+        return RT_OK;
+    } catch (...) {
+        return RT_ERR_OOM;
+    }
+}
+
+/* test hook (not part of radiantium.h): the texel (u, v offsets) and pdf that
+ * infinite light `which` of the uploaded scene samples for each of n uniform
+ * pairs (u[2i] for the column, u[2i + 1] for the row), in the context's light-
+ * sampling mode, computed on the device */
+int rt_debug_env_sample(void* ctx, int which, const float* u, int64_t n, int32_t* texel, float* pdf) {
+    Ctx* c = (Ctx*)ctx;
+    return run(c, [&]() {
+        if (!c->has_scene) throw RtFail(RT_ERR_NO_SCENE, "no scene uploaded");
+        if (which < 0 || which >= c->view.infinite_count || n < 0 || !u || !texel || !pdf)
+            throw RtFail(RT_ERR_INVALID_ARG, "env_sample: bad light or arrays");
+        char* d = nullptr;
+        CK(rt_dev_malloc((void**)&d, (size_t)n * 20 + 16));
+        float2* du = (float2*)d;
+        int2* dt = (int2*)(d + (size_t)n * 8);
+        float* dp = (float*)(d + (size_t)n * 16);
+        cudaError_t e = cudaMemcpyAsync(du, u, (size_t)n * 8, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = rt_launch_env_sample(c->d_view, which, du, n, dt, dp, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(texel, dt, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(pdf, dp, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(d);
+        CK(e);
+    });
 }
 
 /* test hook (not part of radiantium.h): runs rt_detmath (fn 0..7) or CUDA's

@@ -152,6 +152,21 @@ __global__ void k_detmath(int fn, const float* a, const float* b, float* out, in
     out[i] = r;
 }
 
+/* environment-sampling hook: Distribution2D.SampleContinuous's texel and pdf
+ * (as SampleLi uses them) of infinite light `which` for each pair of uniforms,
+ * in the scene's current light-sampling mode */
+__global__ void k_env_sample(const RtSceneView* __restrict__ S, int which, const float2* __restrict__ u, int64_t n,
+                             int2* __restrict__ texel, float* __restrict__ pdf) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const RtDist2D d = S->dists[S->lights[S->infinite_lights[which]].dist];
+    const float2 uv = u[i];
+    float p; int ov, ou;
+    Sample2D(S, d, v2(uv.x, uv.y), &p, &ov, &ou);
+    texel[i] = make_int2(ou, ov);
+    pdf[i] = p;
+}
+
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
@@ -189,5 +204,12 @@ cudaError_t rt_launch_trace(const RtSceneView* S, const rt_ray* rays, int64_t n,
 
 cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream) {
     k_detmath<<<grid_for(n, 256), 256, 0, stream>>>(fn, a, b, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t rt_launch_env_sample(const RtSceneView* S, int which, const float2* u, int64_t n, int2* texel, float* pdf,
+                                 cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_env_sample<<<grid_for(n, 256), 256, 0, stream>>>(S, which, u, n, texel, pdf);
     return cudaGetLastError();
 }

@@ -35,6 +35,8 @@ cudaError_t rt_launch_particle_records(const RtSceneView* S, const RtParams& P, 
 cudaError_t rt_launch_particle_finish(const RtSceneView* S, int64_t npix, const float4* film, float v, float* out,
                                      uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t stream);
 cudaError_t rt_launch_scale(float* v, int64_t n, float s, cudaStream_t stream);
+cudaError_t rt_launch_env_sample(const RtSceneView* S, int which, const float2* u, int64_t n, int2* texel, float* pdf,
+                                 cudaStream_t stream);
 cudaError_t rt_launch_detmath(int fn, const float* a, const float* b, float* out, int64_t n, cudaStream_t stream);
 
 #endif

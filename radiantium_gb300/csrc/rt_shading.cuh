@@ -504,9 +504,32 @@ DF float Sample1D(const float* pdf, const float* cdf, float integ, int n, float 
     *pdfOut = integ > 0 ? __ldg(pdf + *off) / integ : 0;
     return ((float)*off + du) / (float)n;
 }
+/* The alias pick of an n-entry table (built by alias_from_cdf in rt_host.cpp)
+ * for u = k / 2^24, as every NextFloat is: bucket floor(k n / 2^24), kept when
+ * the remainder k n mod 2^24 is below its threshold, else its alias.  The
+ * arithmetic is exact integer arithmetic, so every k lands where the host's
+ * count of the table assumes. */
+DF int AliasPick(const int2* tab, int n, float u) {
+    const uint32_t k = (uint32_t)(u * 16777216.0f);
+    const uint64_t s = (uint64_t)k * (uint32_t)n;
+    const int i = (int)(s >> 24);
+    const int2 e = __ldg(tab + i);
+    return (uint32_t)(s & 0xFFFFFFu) < (uint32_t)e.x ? i : e.y;
+}
 DF void Sample2D(const RtSceneView* S, const RtDist2D& d, V2 u, float* pdf, int* ov, int* ou) {
     float pdf1, pdf0;
     const float* P = S->dist_pool;
+    if (S->env_alias && d.marg_alias >= 0) {
+        /* the same texel pmf and the same pdf arithmetic as the search below;
+         * SampleLi and SampleEmit use only the offsets and the pdf */
+        *ov = AliasPick(S->alias_pool + d.marg_alias, d.nv, u.y);
+        *ou = AliasPick(S->alias_pool + d.cond_alias + (int64_t)(*ov) * d.nu, d.nu, u.x);
+        pdf1 = d.marg_int > 0 ? __ldg(P + d.marg_pdf + *ov) / d.marg_int : 0;
+        const float ci = __ldg(P + d.cond_int + *ov);
+        pdf0 = ci > 0 ? __ldg(P + d.cond_pdf + (int64_t)(*ov) * d.nu + *ou) / ci : 0;
+        *pdf = pdf0 * pdf1;
+        return;
+    }
     Sample1D(P + d.marg_pdf, P + d.marg_cdf, d.marg_int, d.nv, u.y, &pdf1, ov);
     const float* cpdf = P + d.cond_pdf + (int64_t)(*ov) * d.nu;
     const float* ccdf = P + d.cond_cdf + (int64_t)(*ov) * (d.nu + 1);

@@ -132,6 +132,8 @@ struct RtDist2D {
     int64_t cond_int;
     int64_t marg_pdf;
     int64_t marg_cdf;
+    int64_t marg_alias;  /* int2 offsets into the alias pool: the marginal's table (nv */
+    int64_t cond_alias;  /* entries), then nv conditional tables of nu; -1 if none */
     float marg_int;
     int32_t pad;
 };
@@ -168,6 +170,7 @@ struct RtSceneView {
     const int32_t* infinite_lights;
     const RtDist2D* dists;
     const float* dist_pool;
+    const int2* alias_pool;     /* {threshold, alias} per entry of every Distribution1D */
     int32_t light_count;
     int32_t infinite_count;
     int32_t global_medium;
@@ -176,7 +179,7 @@ struct RtSceneView {
                                  * is pushed exactly as the reference pushes it */
     const float4* wnodes;       /* wide nodes of every tree (RT_WIDE_F4 float4 each) */
     int32_t wide_ok;            /* every wide traversal fits the stack: the fast mode may run */
-    int32_t pad_;
+    int32_t env_alias;          /* infinite lights pick texels from their alias tables */
     RtCamera camera;
 };
 

@@ -74,6 +74,26 @@ class Device:
         self._check(self.lib.rt_get_traversal(self.h, C.byref(v)))
         return v.value
 
+    def set_light_sampling(self, mode: int):
+        """N.LIGHT_SAMPLING_CDF (the reference's CDF search) / N.LIGHT_SAMPLING_ALIAS (opt-in alias tables
+        with the same texel pmf) for the infinite lights of this context's scene"""
+        self._check(self.lib.rt_set_light_sampling(self.h, mode))
+
+    def light_sampling(self) -> int:
+        v = C.c_int()
+        self._check(self.lib.rt_get_light_sampling(self.h, C.byref(v)))
+        return v.value
+
+    def env_sample(self, u, which=0):
+        """Texel offsets (column, row) and pdf that infinite light `which` samples for each row
+        (u_column, u_row) of u, computed on the device in the current light-sampling mode."""
+        u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+        texel = np.empty((u.shape[0], 2), np.int32)
+        pdf = np.empty(u.shape[0], np.float32)
+        self._check(self.lib.rt_debug_env_sample(self.h, which, u.ctypes.data, u.shape[0], texel.ctypes.data,
+                                                 pdf.ctypes.data))
+        return texel, pdf
+
     def stats(self) -> dict:
         st = N.Stats()
         self._check(self.lib.rt_get_stats(self.h, C.byref(st)))

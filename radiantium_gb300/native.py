@@ -153,10 +153,11 @@ EXPORTED_SYMBOLS = [
     "rt_abi_version", "rt_create", "rt_destroy", "rt_last_error", "rt_upload_scene",
     "rt_trace_closest", "rt_trace_any", "rt_trace_closest_device", "rt_trace_any_device",
     "rt_render", "rt_render_device", "rt_adjoint_forward", "rt_adjoint_backward", "rt_update_texture", "rt_render_device_noalloc", "rt_render_batch", "rt_render_batch_device", "rt_autotune", "rt_get_stats", "rt_set_counting",
-    "rt_set_renderer", "rt_set_traversal", "rt_get_traversal", "rt_cancel", "rt_render_particles", "rt_render_particles_device",
+    "rt_set_renderer", "rt_set_traversal", "rt_get_traversal", "rt_set_light_sampling", "rt_get_light_sampling", "rt_cancel", "rt_render_particles", "rt_render_particles_device",
 ]
 RENDERER_AUTO, RENDERER_MEGAKERNEL, RENDERER_WAVEFRONT, RENDERER_WAVEFRONT_GRAPH = 0, 1, 2, 3
 TRAVERSAL_EXACT, TRAVERSAL_WIDE = 0, 1
+LIGHT_SAMPLING_CDF, LIGHT_SAMPLING_ALIAS = 0, 1
 MAX_BATCH = 256
 ADJ_MAX_ALPHA = 1024
 MAX_SLOTS = 1 << 21       # path slots in flight (wavefront)
@@ -213,6 +214,14 @@ def _declare(lib):
     lib.rt_set_traversal.argtypes = [vp, C.c_int]
     lib.rt_get_traversal.restype = C.c_int
     lib.rt_get_traversal.argtypes = [vp, C.POINTER(C.c_int)]
+    lib.rt_set_light_sampling.restype = C.c_int
+    lib.rt_set_light_sampling.argtypes = [vp, C.c_int]
+    lib.rt_get_light_sampling.restype = C.c_int
+    lib.rt_get_light_sampling.argtypes = [vp, C.POINTER(C.c_int)]
+    lib.rt_debug_env_sample.restype = C.c_int
+    lib.rt_debug_env_sample.argtypes = [vp, C.c_int, vp, C.c_int64, vp, vp]
+    lib.rt_debug_alias.restype = C.c_int
+    lib.rt_debug_alias.argtypes = [vp, C.c_int, vp]
     lib.rt_cancel.restype = C.c_int
     lib.rt_cancel.argtypes = [vp]
     lib.rt_render_particles.restype = C.c_int
