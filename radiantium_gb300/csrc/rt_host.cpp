@@ -196,7 +196,8 @@ void ensure_wf(Ctx* c, int slots) {
     const size_t n = (size_t)slots, q = 3 * (size_t)slots;
     W.q_o = wf_alloc<float4>(c, q); W.q_d = wf_alloc<float4>(c, q); W.q_meta = wf_alloc<int32_t>(c, q);
     W.active[0] = wf_alloc<int32_t>(c, n); W.active[1] = wf_alloc<int32_t>(c, n);
-    W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint8_t>(c, n); W.mark = wf_alloc<uint8_t>(c, n);
+    W.sorted = wf_alloc<int32_t>(c, n); W.sort_key = wf_alloc<uint16_t>(c, n); W.mark = wf_alloc<uint8_t>(c, n);
+    W.key_count = wf_alloc<int32_t>(c, 2 * WF_SHADE_KEYS);
     W.job = wf_alloc<uint8_t>(c, n);
     W.pix = wf_alloc<int4>(c, n); W.rng_n = wf_alloc<uint32_t>(c, n);
     W.coeff = wf_alloc<float4>(c, n); W.rad = wf_alloc<float4>(c, n);

@@ -1453,12 +1453,12 @@ __global__ void k_wf_active_init(WfState W) {
 /* Code key of an active path: which code the shade kernel will run for it.
  * 0 finished (pending term, then a new sample), 1 missed the scene, 2 hit a
  * medium boundary without a surface, 3 + RT_MAT_* hit that material type,
- * 15 vol_path boundary walks.  The shade key puts the job (mod 16) above it,
+ * 15 vol_path boundary walks.  The shade key puts the job (mod 64) above it,
  * so a batch shades - and then traces - one scene's paths together. */
 DF int shade_key(const WfState& W, int slot) {
     const uint32_t fl = W.flags[slot];
     const int job = W.job[slot];
-    const int jk = (job & 15) << 4;
+    const int jk = (job & 63) << 4;
     if (fl & (F_WTR | F_WIT)) return jk | 15;
     if (fl & F_DONE) return jk;
     const int hs = __float_as_int(W.ext_hit[slot].w);
@@ -1477,7 +1477,7 @@ __global__ void k_wf_phase(WfState W) {
         c->n_closest = 0; c->n_shadow = 0; c->fetch[0] = 0; c->fetch[1] = 0; c->shade_fetch = 0;
         c->n_active[(c->iter & 1) ^ 1] = 0;
     }
-    for (int k = threadIdx.x; k < 2 * WF_SHADE_KEYS; k += blockDim.x) W.ctr->key_count[k] = 0;
+    for (int k = threadIdx.x; k < 2 * WF_SHADE_KEYS; k += blockDim.x) W.key_count[k] = 0;
 }
 
 /* The sort's input order.  While at least one slot in WF_DENSE_SORT is active
@@ -1510,33 +1510,41 @@ __global__ void __launch_bounds__(256) k_wf_sort_count(WfState W) {
         const int slot = sort_input(W, cur, n, i);
         if (slot < 0) continue;
         const int key = shade_key(W, slot);
-        W.sort_key[i] = (uint8_t)key;
+        W.sort_key[i] = (uint16_t)key;
         const unsigned peers = __match_any_sync(__activemask(), key);
-        if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.ctr->key_count + key, __popc(peers));
+        if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(W.key_count + key, __popc(peers));
     }
 }
 
 /* counting-sort scatter: entries of one key stay together, in any order
  * (every path's result is independent of the order paths are shaded in).
  * Each block turns the key counts into bases with a shared-memory scan. */
-static_assert(WF_SHADE_KEYS == 256, "the scatter's scan runs one thread per key in a 256-thread block");
+#define WF_KEYS_PER_THREAD (WF_SHADE_KEYS / 256)
+static_assert(WF_SHADE_KEYS % 256 == 0, "the scatter's scan gives each of 256 threads the same number of keys");
 __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
     __shared__ int base[WF_SHADE_KEYS];
+    __shared__ int part[256];
     const int cur = W.ctr->iter & 1;
     const int n = min(W.ctr->n_active[cur], W.slots);
     const int span = sort_span(W, n);
     if ((int)(blockIdx.x * blockDim.x) >= span) return;
     const int t = threadIdx.x;
-    int v = W.ctr->key_count[t];
-    base[t] = v;
+    /* exclusive scan of the key counts: each thread sums its run of keys,
+     * the 256 sums are scanned (Hillis-Steele), then each run is filled in */
+    int v[WF_KEYS_PER_THREAD], sum = 0;
+#pragma unroll
+    for (int j = 0; j < WF_KEYS_PER_THREAD; j++) { v[j] = W.key_count[t * WF_KEYS_PER_THREAD + j]; sum += v[j]; }
+    part[t] = sum;
     __syncthreads();
-    for (int off = 1; off < WF_SHADE_KEYS; off <<= 1) {      /* inclusive Hillis-Steele scan */
-        const int add = t >= off ? base[t - off] : 0;
+    for (int off = 1; off < 256; off <<= 1) {
+        const int add = t >= off ? part[t - off] : 0;
         __syncthreads();
-        base[t] += add;
+        part[t] += add;
         __syncthreads();
     }
-    base[t] -= v;                                           /* exclusive */
+    int run = part[t] - sum;
+#pragma unroll
+    for (int j = 0; j < WF_KEYS_PER_THREAD; j++) { base[t * WF_KEYS_PER_THREAD + j] = run; run += v[j]; }
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
     for (int i0 = blockIdx.x * blockDim.x; i0 < span; i0 += gridDim.x * blockDim.x) {
@@ -1548,7 +1556,7 @@ __global__ void __launch_bounds__(256) k_wf_sort_scatter(WfState W) {
         const unsigned peers = __match_any_sync(__activemask(), key);
         const int leader = __ffs(peers) - 1;
         int first = 0;
-        if ((int)lane == leader) first = atomicAdd(W.ctr->key_count + WF_SHADE_KEYS + key, __popc(peers));
+        if ((int)lane == leader) first = atomicAdd(W.key_count + WF_SHADE_KEYS + key, __popc(peers));
         first = __shfl_sync(peers, first, leader);
         const int dst = base[key] + first + __popc(peers & ((1u << lane) - 1u));
         if (in_bounds(W, dst, W.slots)) W.sorted[dst] = slot;

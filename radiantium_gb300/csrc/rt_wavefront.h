@@ -25,7 +25,7 @@ enum { WF_RAY_SPLAT = 2 };
 
 #define WF_MAX_JOBS 256            /* job index is 8 bits in the ray-queue meta word */
 #define WF_MAX_SLOTS (1 << 21)     /* slot index is 21 bits in the ray-queue meta word */
-#define WF_SHADE_KEYS 256          /* shade key: (job mod 16) * 16 + the path's code key (0..15) */
+#define WF_SHADE_KEYS 1024         /* shade key: (job mod 64) * 16 + the path's code key (0..15) */
 #ifndef WF_ITER_CAP
 #define WF_ITER_CAP (1 << 20)      /* bounce iterations of one round before a run gives up */
 #endif
@@ -65,7 +65,6 @@ struct WfCounters {
     int32_t fetch[2];              /* next closest / shadow queue entry to hand out */
     int32_t shade_fetch;           /* next sorted entry to shade (resident-grid shading) */
     int32_t pad;
-    int32_t key_count[2 * WF_SHADE_KEYS];   /* per shade key: entries, scatter cursor */
 };
 
 /* structure-of-arrays path state; every array has one entry per path slot
@@ -85,7 +84,8 @@ struct WfState {
     const WfJob* jobs;
     /* active slot lists by iteration parity, and the list regrouped by shade key */
     int32_t* active[2];
-    int32_t* sorted; uint8_t* sort_key;
+    int32_t* sorted; uint16_t* sort_key;
+    int32_t* key_count;      /* per shade key: entries, then scatter cursors (2 * WF_SHADE_KEYS) */
     uint8_t* mark;           /* per slot: 1 + the active list (iteration parity) it is on, 0 if none */
     /* path state */
     uint8_t* job;            /* job of the slot's path */
