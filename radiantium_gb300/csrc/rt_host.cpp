@@ -108,6 +108,7 @@ struct Ctx {
     int64_t sample_budget = 1 << 24;          /* samples per launch (sample buffer = 12 B each) */
     std::vector<cudaEvent_t> events;           /* per-launch timing of the path-tracing kernel */
     int renderer = RT_RENDERER_AUTO;
+    WfFork fork{};                             /* side stream for the shadow-ray kernel (rt_wf_trace) */
     int traversal = RT_TRAVERSAL_EXACT;        /* rt_set_traversal */
     int light_sampling = RT_LIGHT_SAMPLING_CDF; /* rt_set_light_sampling */
     int wf_iter_cap = WF_ITER_CAP;             /* bounce iterations of one wavefront round (test hook) */
@@ -188,7 +189,7 @@ void free_wf(Ctx* c) {
     c->wf_slots = 0;
 }
 
-/* path-state arrays for `slots` paths in flight (about 300 bytes per slot) */
+/* path-state arrays for `slots` paths in flight (about 560 bytes per slot: 1.1 GiB at 2 Mi slots) */
 void ensure_wf(Ctx* c, int slots) {
     if (c->wf_slots >= slots) return;
     free_wf(c);
@@ -992,7 +993,7 @@ void wf_round(Ctx* c, const WfState& W, cudaStream_t s, bool use_graph, const Wf
         if (c->h_ctr->iter >= W.iter_cap) throw RtFail(RT_ERR_ITER_CAP, "wavefront: bounce iteration cap reached (WF_ITER_CAP)");
         NvtxRange nvtx_iter("rt.wavefront_iteration");
         CK(cudaEventRecord(c->events[0], s));
-        CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, m.deep, m.wide));
+        CK(rt_wf_trace(W, c->status, c->stats, c->counting, s, m.deep, m.wide, &c->fork));
         CK(cudaEventRecord(c->events[1], s));
         CK(cudaEventRecord(c->events[2], s));
         CK(rt_wf_shade(W, c->h_ctr->n_active[c->h_ctr->iter & 1], c->status, c->stats, c->counting, 0, false, s,
@@ -1249,7 +1250,7 @@ void ensure_wf_graph(Ctx* c, const WfState& W, bool vol, bool particle, bool sor
     cudaGraph_t body = np.conditional.phGraph_out[0];
     CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     uint64_t launches = 0;
-    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream, deep, wide);
+    cudaError_t e1 = rt_wf_trace(W, c->status, c->stats, c->counting, c->stream, deep, wide, &c->fork);
     cudaError_t e2 = rt_wf_shade(W, -1, c->status, c->stats, c->counting, loop, true, c->stream, &launches,
                                  WF_PASS_RENDER, nullptr, vol, particle, sort);
     cudaGraph_t captured = nullptr;
@@ -1649,10 +1650,13 @@ int rt_create(int device, void** out_ctx) {
     c->device = device;
     int rc = run(c, [&]() {
         CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&c->fork.side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->fork.fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->fork.join, cudaEventDisableTiming));
         CK(rt_dev_malloc((void**)&c->status, 4));
         CK(rt_dev_malloc((void**)&c->stats, 8 * sizeof(unsigned long long)));
     });
-    if (rc != RT_OK) { delete c; return rc; }
+    if (rc != RT_OK) { rt_destroy(c); return rc; }
     *out_ctx = c;
     return RT_OK;
 }
@@ -1680,6 +1684,9 @@ void rt_destroy(void* ctx) {
     if (c->d_jobs) cudaFree(c->d_jobs);
     if (c->h_jobs) cudaFreeHost(c->h_jobs);
     for (cudaEvent_t e : c->events) cudaEventDestroy(e);
+    if (c->fork.fork) cudaEventDestroy(c->fork.fork);
+    if (c->fork.join) cudaEventDestroy(c->fork.join);
+    if (c->fork.side) cudaStreamDestroy(c->fork.side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

@@ -1603,7 +1603,7 @@ cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle) {
 }
 
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
-                        bool deep, bool wide) {
+                        bool deep, bool wide, const WfFork* fork) {
     static const int closest_blocks[4] = {resident_blocks(k_wf_trace_closest<false, false>, RT_TRACE_BLOCK),
                                           resident_blocks(k_wf_trace_closest<true, false>, RT_TRACE_BLOCK),
                                           resident_blocks(k_wf_trace_closest<false, true>, RT_TRACE_BLOCK),
@@ -1613,21 +1613,32 @@ cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* 
                                          resident_blocks(k_wf_trace_shadow<false, true>, RT_TRACE_BLOCK),
                                          resident_blocks(k_wf_trace_shadow<true, true>, RT_TRACE_BLOCK)};
     const int v = (deep ? 1 : 0) + (wide ? 2 : 0);
+    cudaError_t e = cudaSuccess;
+    if (fork) {
+        e = cudaEventRecord(fork->fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(fork->side, fork->fork, 0);
+        if (e != cudaSuccess) return e;
+    }
     switch (v) {
     case 0: k_wf_trace_closest<false, false><<<closest_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
     case 1: k_wf_trace_closest<true, false><<<closest_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
     case 2: k_wf_trace_closest<false, true><<<closest_blocks[2], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
     default: k_wf_trace_closest<true, true><<<closest_blocks[3], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
     }
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    const cudaStream_t ss = fork ? fork->side : s;
     switch (v) {
-    case 0: k_wf_trace_shadow<false, false><<<shadow_blocks[0], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
-    case 1: k_wf_trace_shadow<true, false><<<shadow_blocks[1], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
-    case 2: k_wf_trace_shadow<false, true><<<shadow_blocks[2], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
-    default: k_wf_trace_shadow<true, true><<<shadow_blocks[3], RT_TRACE_BLOCK, 0, s>>>(W, status, stats, counting); break;
+    case 0: k_wf_trace_shadow<false, false><<<shadow_blocks[0], RT_TRACE_BLOCK, 0, ss>>>(W, status, stats, counting); break;
+    case 1: k_wf_trace_shadow<true, false><<<shadow_blocks[1], RT_TRACE_BLOCK, 0, ss>>>(W, status, stats, counting); break;
+    case 2: k_wf_trace_shadow<false, true><<<shadow_blocks[2], RT_TRACE_BLOCK, 0, ss>>>(W, status, stats, counting); break;
+    default: k_wf_trace_shadow<true, true><<<shadow_blocks[3], RT_TRACE_BLOCK, 0, ss>>>(W, status, stats, counting); break;
     }
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !fork) return e;
+    e = cudaEventRecord(fork->join, fork->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fork->join, 0);
+    return e;
 }
 
 cudaError_t rt_wf_shade(const WfState& W, int n_hint, uint32_t* status, unsigned long long* stats, bool counting,

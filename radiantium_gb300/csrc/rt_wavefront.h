@@ -134,8 +134,16 @@ cudaError_t rt_wf_start(const WfState& W, cudaStream_t s, bool particle = false)
 #ifndef RT_DEEP_TREE
 #define RT_DEEP_TREE 16
 #endif
+/* With `fork`, the shadow-ray kernel runs on fork->side, joined back into `s`
+ * before the call returns (in stream order): its blocks take the SM slots the
+ * closest-hit kernel's blocks free as its queue runs dry, so neither kernel's
+ * tail leaves the GPU idle. */
+struct WfFork {
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+};
 cudaError_t rt_wf_trace(const WfState& W, uint32_t* status, unsigned long long* stats, bool counting, cudaStream_t s,
-                        bool deep = false, bool wide = false);
+                        bool deep = false, bool wide = false, const WfFork* fork = nullptr);
 /* Shades the active paths (`particle`: light-tracer particles) - regrouped by
  * shade key first with `sort` - then advances the iteration; with `loop` set
  * (inside a captured while-loop), also sets the loop's condition to "paths
