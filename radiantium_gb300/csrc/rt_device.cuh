@@ -503,6 +503,42 @@ DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, in
     const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
     const int4 ra = __ldg(reinterpret_cast<const int4*>(np + 4)), rb = __ldg(reinterpret_cast<const int4*>(np + 5));
     const uint32_t meta = __float_as_uint(w0.w);
+    const float kWiden = 9.5367431640625e-07f;   /* 2^-20 */
+    uint32_t key[8];
+    /* The split form below, q (s/d) + (p - o)/d, needs both terms finite: for
+     * a direction component of zero (or so small that 1/d times a node origin
+     * or grid step overflows) it would add infinities of opposite sign, the
+     * NaN would drop that axis from the test (fmaxf / fminf ignore it) and
+     * every box would count as unbounded along it.  Such rays decode each
+     * child box (outward-widened) and run the exact traversal's own slab
+     * test, SlabA, on it: the box contains the reference's box, so the test
+     * accepts a superset of what the reference's test accepts, with its
+     * IEEE semantics for the infinite 1/d. */
+    const float kHuge = 3.9614081257132169e28f;  /* 2^95 */
+    if (fabsf(r.InvD.x) >= kHuge || fabsf(r.InvD.y) >= kHuge || fabsf(r.InvD.z) >= kHuge) {
+        const float sx = __uint_as_float((meta & 0xffu) << 23), sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
+        const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
+        const uint32_t lx[2] = {__float_as_uint(w1.x), __float_as_uint(w1.y)}, hx[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
+        const uint32_t ly[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)}, hy[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
+        const uint32_t lz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)}, hz[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
+        auto lo = [kWiden](float v) { return v - fabsf(v) * kWiden - 1e-30f; };
+        auto hi = [kWiden](float v) { return v + fabsf(v) * kWiden + 1e-30f; };
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int b = k & 3, h = k >> 2;
+            float tmin = 0.0f;
+            const bool hit = k < (int)(meta >> 24) &&
+                             SlabA(lo(w0.x + wq(lx[h], b) * sx), lo(w0.y + wq(ly[h], b) * sy), lo(w0.z + wq(lz[h], b) * sz),
+                                   hi(w0.x + wq(hx[h], b) * sx), hi(w0.y + wq(hy[h], b) * sy), hi(w0.z + wq(hz[h], b) * sz),
+                                   r, &tmin) &&
+                             __fmaf_rn(-fabsf(tmin), kWiden, tmin) <= r.MaxT;
+            /* the entry distance widened as in the split form, so a flat box met
+             * at exactly the current MaxT is still visited (ties are found) */
+            const float tw = __fmaf_rn(-fabsf(tmin), kWiden, tmin);
+            const float te = tw > 0.0f ? tw : 0.0f;
+            key[k] = hit ? ((__float_as_uint(te) & ~7u) | (uint32_t)k) : 0xffffffffu;
+        }
+    } else {
     const float ax = __uint_as_float((meta & 0xffu) << 23) * r.InvD.x;
     const float ay = __uint_as_float(((meta >> 8) & 0xffu) << 23) * r.InvD.y;
     const float az = __uint_as_float(((meta >> 16) & 0xffu) << 23) * r.InvD.z;
@@ -515,8 +551,6 @@ DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, in
     const uint32_t gy0 = __float_as_uint(fy ? w2.x : w2.z), gy1 = __float_as_uint(fy ? w2.y : w2.w);
     const uint32_t nz0 = __float_as_uint(fz ? w3.z : w3.x), nz1 = __float_as_uint(fz ? w3.w : w3.y);
     const uint32_t gz0 = __float_as_uint(fz ? w3.x : w3.z), gz1 = __float_as_uint(fz ? w3.y : w3.w);
-    const float kWiden = 9.5367431640625e-07f;   /* 2^-20 */
-    uint32_t key[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const int b = k & 3;
@@ -529,6 +563,7 @@ DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, in
         const bool hit = k < (int)(meta >> 24) && tlo <= thi && thi >= 0.0f && tlo <= r.MaxT;
         const float te = tlo > 0.0f ? tlo : 0.0f;
         key[k] = hit ? ((__float_as_uint(te) & ~7u) | (uint32_t)k) : 0xffffffffu;
+    }
     }
     /* Batcher's odd-even merge sort of eight keys (19 compare-exchanges) */
     ucas(key[0], key[1]); ucas(key[2], key[3]); ucas(key[4], key[5]); ucas(key[6], key[7]);

@@ -105,14 +105,8 @@ def _trace(dev, rays, mode):
         dev.set_traversal(N.TRAVERSAL_EXACT)
 
 
-@pytest.mark.parametrize("name", ["cornell", "zoo", "C2", "C3", "C4"])
-def test_wide_hits_equal_exact_up_to_ties_and_slab_misses(dev, name):
-    s, _ = _scene(name)
-    dev.upload(s)
-    n = 1 << 20 if name in ("C2", "C3") else 200000
-    rays = _rays(s, n, 7)
-    e, ea = _trace(dev, rays, N.TRAVERSAL_EXACT)
-    w, wa = _trace(dev, rays, N.TRAVERSAL_WIDE)
+def _classify(name, s, rays, e, w, ea, wa):
+    """Checks the contract above for one batch; returns (ties, slab misses, NaN culls)."""
     same = (e["prim"] == w["prim"]) & (e["sub"] == w["sub"])
     # the same primitive: the same arithmetic
     for k in ("t", "u", "v"):
@@ -133,14 +127,87 @@ def test_wide_hits_equal_exact_up_to_ties_and_slab_misses(dev, name):
             g = inst.get(int(e["prim"][i]))
             assert g is not None and _nan_model_maxt(rays[i], g), (name, i, rays[i], e[i], w[i])
             nan_culls += 1
-    print(f"{name}: {rays.size} rays, {ties} ties (within {TIE_ULP} ulp), {misses} reference slab misses, "
-          f"{nan_culls} instances culled by a NaN model-space MaxT")
     assert ties <= MAX_TIES * rays.size, (name, ties)
     assert misses <= MAX_MISSES * rays.size, (name, misses)
     # any hit: a superset of the exact answers
     assert not (ea.astype(bool) & ~wa.astype(bool)).any()
     assert int((wa.astype(bool) & ~ea.astype(bool)).sum()) <= MAX_MISSES * rays.size
+    return ties, misses, nan_culls
+
+
+@pytest.mark.parametrize("name", ["cornell", "zoo", "C2", "C3", "C4"])
+def test_wide_hits_equal_exact_up_to_ties_and_slab_misses(dev, name):
+    s, _ = _scene(name)
+    dev.upload(s)
+    n = 1 << 20 if name in ("C2", "C3") else 200000
+    rays = _rays(s, n, 7)
+    e, ea = _trace(dev, rays, N.TRAVERSAL_EXACT)
+    w, wa = _trace(dev, rays, N.TRAVERSAL_WIDE)
+    ties, misses, nan_culls = _classify(name, s, rays, e, w, ea, wa)
+    print(f"{name}: {rays.size} rays, {ties} ties (within {TIE_ULP} ulp), {misses} reference slab misses, "
+          f"{nan_culls} instances culled by a NaN model-space MaxT")
     assert (e["prim"] >= 0).sum() > rays.size // 10
+
+
+def _axis_rays(s, n, seed):
+    """Rays whose direction has exactly-zero components: a third along the six
+    axes (two zeros, signed zeros included), the rest in the three coordinate
+    planes (one zero), from points inside the scene's box."""
+    orc = OracleScene(s)
+    try:
+        root = orc.bvh(-1)["bounds"][0].astype(np.float64)
+    finally:
+        orc.close()
+    rng = np.random.default_rng(seed)
+    lo, hi = root[:3], root[3:]
+    o = lo + rng.random((n, 3)) * (hi - lo)
+    d = np.zeros((n, 3))
+    k = n // 3
+    axis = rng.integers(0, 3, k)
+    d[np.arange(k), axis] = rng.choice([-1.0, 1.0], k)
+    a = rng.random(n - k) * 2 * np.pi
+    zero = rng.integers(0, 3, n - k)
+    for z in range(3):
+        m = zero == z
+        u, v = [c for c in range(3) if c != z]
+        d[k:][m, u] = np.cos(a[m])
+        d[k:][m, v] = np.sin(a[m])
+    rays = np.zeros(n, dtype=N.ray_dtype())
+    rays["o"] = o.astype(np.float32)
+    dd = d.astype(np.float32)
+    dd[dd == 0] = np.where(rng.random(int((dd == 0).sum())) < 0.5, 0.0, -0.0).astype(np.float32)
+    rays["d"] = dd
+    rays["min_t"] = 1e-4
+    rays["max_t"] = np.float32(3.4028234663852886e38)
+    return rays
+
+
+@pytest.mark.parametrize("name", ["cornell", "C2", "C3"])
+def test_wide_axis_parallel_rays(dev, name):
+    """Directions with zero components (1/d infinite): the same contract, and
+    the wide traversal visits fewer nodes than the exact one - a zero
+    component must not make its boxes unbounded along that axis."""
+    s, _ = _scene(name)
+    dev.upload(s)
+    rays = _axis_rays(s, 200000, 13)
+    visits = {}
+    res = {}
+    dev.set_counting(True)
+    try:
+        for mode in (N.TRAVERSAL_EXACT, N.TRAVERSAL_WIDE):
+            dev.set_traversal(mode)
+            res[mode] = dev.trace_closest(rays)
+            visits[mode] = dev.stats()["node_visits"]
+            res[mode] = (res[mode], dev.trace_any(rays))
+    finally:
+        dev.set_counting(False)
+        dev.set_traversal(N.TRAVERSAL_EXACT)
+    (e, ea), (w, wa) = res[N.TRAVERSAL_EXACT], res[N.TRAVERSAL_WIDE]
+    ties, misses, nan_culls = _classify(name, s, rays, e, w, ea, wa)
+    print(f"{name}: {ties} ties, {misses} slab misses, {nan_culls} NaN culls; node visits per ray exact "
+          f"{visits[N.TRAVERSAL_EXACT] / rays.size:.1f}, wide {visits[N.TRAVERSAL_WIDE] / rays.size:.1f}")
+    assert (e["prim"] >= 0).sum() > rays.size // 10
+    assert visits[N.TRAVERSAL_WIDE] < visits[N.TRAVERSAL_EXACT]
 
 
 @pytest.mark.parametrize("name,spp", [("C2", 2), ("C3", 2), ("zoo", 16)])
