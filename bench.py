@@ -245,6 +245,42 @@ def profiled_traffic(name, key="bytes_per_sample"):
     return None
 
 
+def cpu_baseline_batch(scenes, step_settings, target_s, threads=0):
+    """The CPU oracle over every scene of the batch: each scene timed on its own
+    spread-tile sample (about target_s / n seconds each, all host cores), and
+    the rates combined with one batch step's sample counts - the CPU time of a
+    step is the sum over scenes of (the scene's samples in the step / its rate)."""
+    from oracle.oracle import OracleScene
+    cores = threads or os.cpu_count() or 1
+    # at least half a second per scene: a tile call's fixed cost must not count
+    per = max(target_s / len(scenes), 0.5)
+    step_samples, cpu_s, sampled, timed_s, build_s = 0, 0.0, 0, 0.0, 0.0
+    for (scene, _), st in zip(scenes, step_settings):
+        t0 = time.perf_counter()
+        orc = OracleScene(scene)
+        build_s += time.perf_counter() - t0
+        size, tiles = cpu_tiles(scene)
+        t0 = time.perf_counter()
+        oracle_tiles(orc, st, size, tiles, 16, 0, cores)
+        t16 = time.perf_counter() - t0
+        # samples beyond the step's own spp (the next sample indices of the same
+        # pixels), so that every scene's sample is long enough to time
+        spp = int(max(16, min(4096, 16 * per / max(t16, 1e-3))))
+        t0 = time.perf_counter()
+        n = oracle_tiles(orc, st, size, tiles, spp, 16, cores)
+        dt = time.perf_counter() - t0
+        orc.close()
+        s_step = scene.camera.width * scene.camera.height * st.spp
+        step_samples += s_step
+        cpu_s += s_step * dt / n
+        sampled += n
+        timed_s += dt
+    return {"value": step_samples / cpu_s, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": (f"every scene of the batch: {CPU_GRID * CPU_GRID} tiles of up to {CPU_TILE}x{CPU_TILE} "
+                       f"pixels spread over each film, {sampled} samples in all ({timed_s:.1f} s; oracle scene "
+                       f"builds {build_s:.1f} s not timed); the scenes' rates weighted by a batch step's samples")}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -841,9 +877,7 @@ def batch_line(args, rank, world, local, dist):
     peak, peak_src = measured_peak()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        s0, st0 = scenes[1]
-        cpu = cpu_baseline(s0, st0, args.cpu_seconds)
-        cpu["sample"] = "scene 1 of the batch: " + cpu["sample"]
+        cpu = cpu_baseline_batch(scenes, batch_step_settings(scenes, base), args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
