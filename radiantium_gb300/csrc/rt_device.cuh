@@ -505,44 +505,26 @@ DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, in
     const uint32_t meta = __float_as_uint(w0.w);
     const float kWiden = 9.5367431640625e-07f;   /* 2^-20 */
     uint32_t key[8];
-    /* The split form below, q (s/d) + (p - o)/d, needs both terms finite: for
-     * a direction component of zero (or so small that 1/d times a node origin
-     * or grid step overflows) it would add infinities of opposite sign, the
-     * NaN would drop that axis from the test (fmaxf / fminf ignore it) and
-     * every box would count as unbounded along it.  Such rays decode each
-     * child box (outward-widened) and run the exact traversal's own slab
-     * test, SlabA, on it: the box contains the reference's box, so the test
-     * accepts a superset of what the reference's test accepts, with its
-     * IEEE semantics for the infinite 1/d. */
-    const float kHuge = 3.9614081257132169e28f;  /* 2^95 */
-    if (fabsf(r.InvD.x) >= kHuge || fabsf(r.InvD.y) >= kHuge || fabsf(r.InvD.z) >= kHuge) {
-        const float sx = __uint_as_float((meta & 0xffu) << 23), sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
-        const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
-        const uint32_t lx[2] = {__float_as_uint(w1.x), __float_as_uint(w1.y)}, hx[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
-        const uint32_t ly[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)}, hy[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
-        const uint32_t lz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)}, hz[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
-        auto lo = [kWiden](float v) { return v - fabsf(v) * kWiden - 1e-30f; };
-        auto hi = [kWiden](float v) { return v + fabsf(v) * kWiden + 1e-30f; };
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const int b = k & 3, h = k >> 2;
-            float tmin = 0.0f;
-            const bool hit = k < (int)(meta >> 24) &&
-                             SlabA(lo(w0.x + wq(lx[h], b) * sx), lo(w0.y + wq(ly[h], b) * sy), lo(w0.z + wq(lz[h], b) * sz),
-                                   hi(w0.x + wq(hx[h], b) * sx), hi(w0.y + wq(hy[h], b) * sy), hi(w0.z + wq(hz[h], b) * sz),
-                                   r, &tmin) &&
-                             __fmaf_rn(-fabsf(tmin), kWiden, tmin) <= r.MaxT;
-            /* the entry distance widened as in the split form, so a flat box met
-             * at exactly the current MaxT is still visited (ties are found) */
-            const float tw = __fmaf_rn(-fabsf(tmin), kWiden, tmin);
-            const float te = tw > 0.0f ? tw : 0.0f;
-            key[k] = hit ? ((__float_as_uint(te) & ~7u) | (uint32_t)k) : 0xffffffffu;
-        }
-    } else {
-    const float ax = __uint_as_float((meta & 0xffu) << 23) * r.InvD.x;
-    const float ay = __uint_as_float(((meta >> 8) & 0xffu) << 23) * r.InvD.y;
-    const float az = __uint_as_float(((meta >> 16) & 0xffu) << 23) * r.InvD.z;
-    const float bx = (w0.x - r.O.x) * r.InvD.x, by = (w0.y - r.O.y) * r.InvD.y, bz = (w0.z - r.O.z) * r.InvD.z;
+    /* 1/d clamped to +-2^95.  The split form q (s/d) + (p - o)/d needs both
+     * terms finite: for a direction component of zero (or so small that 1/d
+     * times a grid step or node origin overflows) it would add infinities of
+     * opposite sign, and fmaxf / fminf would drop the NaN - every box would
+     * count as unbounded along that axis and the traversal would visit most
+     * of the tree.  Clamped, the plane distances of such an axis are 0 or
+     * +-huge with the sign of (plane - origin), so the test keeps exactly the
+     * boxes whose quantised slab contains the origin's coordinate.  A
+     * quantised box contains its exact box with a grid step to spare, so an
+     * origin on a quantised plane lies outside the exact box, where the
+     * reference's slab test (which ignores only NaN bounds) rejects it too:
+     * the test still accepts a superset of the reference's boxes. */
+    const float kClamp = 3.9614081257132169e28f;   /* 2^95 */
+    const float ix = fminf(fmaxf(r.InvD.x, -kClamp), kClamp);
+    const float iy = fminf(fmaxf(r.InvD.y, -kClamp), kClamp);
+    const float iz = fminf(fmaxf(r.InvD.z, -kClamp), kClamp);
+    const float ax = __uint_as_float((meta & 0xffu) << 23) * ix;
+    const float ay = __uint_as_float(((meta >> 8) & 0xffu) << 23) * iy;
+    const float az = __uint_as_float(((meta >> 16) & 0xffu) << 23) * iz;
+    const float bx = (w0.x - r.O.x) * ix, by = (w0.y - r.O.y) * iy, bz = (w0.z - r.O.z) * iz;
     /* near and far planes per axis by the direction's sign: words of children 0-3 and 4-7 */
     const bool fx = r.InvD.x < 0, fy = r.InvD.y < 0, fz = r.InvD.z < 0;
     const uint32_t nx0 = __float_as_uint(fx ? w1.z : w1.x), nx1 = __float_as_uint(fx ? w1.w : w1.y);
@@ -563,7 +545,6 @@ DF int VisitWideNode(const RtSceneView* S, int node, const Ray& r, Stk stack, in
         const bool hit = k < (int)(meta >> 24) && tlo <= thi && thi >= 0.0f && tlo <= r.MaxT;
         const float te = tlo > 0.0f ? tlo : 0.0f;
         key[k] = hit ? ((__float_as_uint(te) & ~7u) | (uint32_t)k) : 0xffffffffu;
-    }
     }
     /* Batcher's odd-even merge sort of eight keys (19 compare-exchanges) */
     ucas(key[0], key[1]); ucas(key[2], key[3]); ucas(key[4], key[5]); ucas(key[6], key[7]);
