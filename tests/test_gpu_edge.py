@@ -90,6 +90,47 @@ def test_degenerate_rays(dev, name):
     assert np.array_equal(got_a.astype(np.uint8), want_a.astype(np.uint8))
 
 
+@pytest.mark.parametrize("name", ["cornell", "instanced", "zoo"])
+def test_axis_parallel_rays_match_oracle(dev, name):
+    """200 k rays with exactly-zero direction components (along the axes and in
+    the coordinate planes, signed zeros included): 1/d is infinite, and the
+    slab test's IEEE semantics (BoundingBox3F.cs:155-176; 0 * inf is NaN, which
+    its comparisons ignore) decide which boxes are entered.  Hits, tie flags
+    and traversal counters equal the oracle's."""
+    from tests.test_gpu_wide_traversal import _axis_rays
+    if name == "cornell":
+        s, _ = procedural.cornell_box(32, 32)
+    elif name == "zoo":
+        s, _ = procedural.material_zoo(32, 32)
+    else:
+        s, _ = procedural.instanced_spheres(32, 32, sphere_n=12, grid=4, env_w=32, env_h=16)
+    rays = _axis_rays(s, 200000, 17)
+    dev.upload(s)
+    orc = OracleScene(s)
+    try:
+        want_h, want_hc = orc.trace_closest(rays, stats=True)
+        want_a, want_ac = orc.trace_any(rays, stats=True)
+    finally:
+        orc.close()
+    dev.set_counting(True)
+    try:
+        got_h = dev.trace_closest(rays)
+        got_hc = dev.stats()
+        got_a = dev.trace_any(rays)
+        got_ac = dev.stats()
+    finally:
+        dev.set_counting(False)
+    for k in ("prim", "sub", "flags"):
+        assert np.array_equal(got_h[k], want_h[k]), k
+    for k in ("t", "u", "v"):
+        assert np.array_equal(_bits(got_h[k]), _bits(want_h[k])), k
+    assert np.array_equal(got_a.astype(np.uint8), want_a.astype(np.uint8))
+    for k in ("node_visits", "prim_tests", "instance_visits"):
+        assert got_hc[k] == want_hc[k], ("closest", k, got_hc[k], want_hc[k])
+        assert got_ac[k] == want_ac[k], ("any", k, got_ac[k], want_ac[k])
+    assert (want_h["prim"] >= 0).sum() > rays.size // 10
+
+
 def test_empty_ray_batch(dev):
     s, _ = procedural.cornell_box(16, 16)
     dev.upload(s)
