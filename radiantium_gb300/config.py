@@ -190,9 +190,11 @@ class GpuRenderer:
     counters behave like BlockBasedRenderer's blocks."""
 
     def __init__(self, scene: SceneDesc, settings: RenderSettings, device: int = 0, passes: int = 0,
-                 particle_count: int = 0):
+                 particle_count: int = 0, traversal: int = N.TRAVERSAL_EXACT,
+                 light_sampling: int = N.LIGHT_SAMPLING_CDF):
         self.scene, self.settings, self.device = scene, settings, device
         self.particle_count = particle_count
+        self.traversal, self.light_sampling = traversal, light_sampling
         work = particle_count if settings.integrator == N.INTEGRATOR_PARTICLE else settings.spp
         self.passes = passes or min(work, 16)
         self._target = np.zeros((scene.camera.width, scene.camera.height, 3), dtype=np.float32)
@@ -254,6 +256,8 @@ class GpuRenderer:
         try:
             with Device(self.device) as dev:
                 self._dev = dev
+                dev.set_traversal(self.traversal)
+                dev.set_light_sampling(self.light_sampling)
                 dev.upload(self.scene)
                 st = self.settings
                 acc = np.zeros_like(self._target, dtype=np.float64)
@@ -290,6 +294,20 @@ class GpuRenderer:
             done += k
             self._done += 1
             self._target[...] = (acc / done).astype(np.float32)
+
+
+def gpu_modes(rc: ConfigParams) -> dict:
+    """The GPU renderer's own options in the "renderer" object (no reference
+    counterpart; the reference ignores keys it does not read): "traversal"
+    "exact" (default) or "wide", "light_sampling" "cdf" (default) or "alias"."""
+    trav = {"exact": N.TRAVERSAL_EXACT, "wide": N.TRAVERSAL_WIDE}
+    ls = {"cdf": N.LIGHT_SAMPLING_CDF, "alias": N.LIGHT_SAMPLING_ALIAS}
+    t, l = rc.str("traversal", "exact"), rc.str("light_sampling", "cdf")
+    if t not in trav:
+        raise ValueError(f"renderer.traversal: {t!r} is not one of {sorted(trav)}")
+    if l not in ls:
+        raise ValueError(f"renderer.light_sampling: {l!r} is not one of {sorted(ls)}")
+    return {"traversal": trav[t], "light_sampling": ls[l]}
 
 
 class RendererBuilder:
@@ -571,11 +589,13 @@ class RendererBuilder:
             raise NotImplementedError(f"integrator {None if ic is None else ic.str('type', None)}")
         settings = self.integrators[ic.str("type", None)](self, ic)
         rc = self.renderer_cfg if self.renderer_cfg is not None else ConfigParams()
+        modes = gpu_modes(rc)
         if settings.integrator == N.INTEGRATOR_PARTICLE:
             # the renderer named by the integrator (AdjointParticleIntegrator.cs:15, RendererBuilder.cs:523)
-            return GpuRenderer(s, settings, device, particle_count=self.renderers["adjoint_particle"](self, rc)[0])
+            return GpuRenderer(s, settings, device, particle_count=self.renderers["adjoint_particle"](self, rc)[0],
+                               **modes)
         settings = settings.replace(spp=self.renderers["block_based"](self, rc)[0])
-        return GpuRenderer(s, settings, device)
+        return GpuRenderer(s, settings, device, **modes)
 
 
 def load_scene_file(path: str, device: int = 0) -> GpuRenderer:

@@ -98,6 +98,22 @@ def test_particle_scene_selects_the_particle_renderer(tmp_path):
     assert np.isfinite(img).all() and img.mean() > 0.0
 
 
+def test_gpu_renderer_mode_options(tmp_path):
+    """The GPU renderer's own "renderer" keys: the opt-in wide traversal and
+    alias-table env sampling; the reference's defaults when absent."""
+    r = load_scene_file(_scene_file(tmp_path, {"type": "path"}, {"type": "gpu_wavefront", "spp": 4}))
+    assert (r.traversal, r.light_sampling) == (N.TRAVERSAL_EXACT, N.LIGHT_SAMPLING_CDF)
+    r = load_scene_file(_scene_file(tmp_path, {"type": "path"},
+                                    {"type": "gpu_wavefront", "spp": 4, "traversal": "wide",
+                                     "light_sampling": "alias"}))
+    assert (r.traversal, r.light_sampling) == (N.TRAVERSAL_WIDE, N.LIGHT_SAMPLING_ALIAS)
+    r = load_scene_file(_scene_file(tmp_path, {"type": "adjoint_particle"}, {"light_sampling": "alias"}))
+    assert r.light_sampling == N.LIGHT_SAMPLING_ALIAS
+    for bad in ({"traversal": "bvh4"}, {"light_sampling": "power"}):
+        with pytest.raises(ValueError):
+            load_scene_file(_scene_file(tmp_path, {"type": "path"}, dict(bad, spp=4)))
+
+
 def test_particle_count_default(tmp_path):
     r = load_scene_file(_scene_file(tmp_path, {"type": "adjoint_particle"}, {}))
     assert r.particle_count == 16384      # RendererBuilder.cs:38

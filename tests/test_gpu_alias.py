@@ -187,3 +187,28 @@ def test_light_sampling_arguments(dev):
     with pytest.raises(N.RTError) as e:
         dev.env_sample(np.zeros((4, 2), np.float32))   # no infinite light
     assert e.value.code == N.RT_ERR_INVALID_ARG
+
+
+def test_scene_file_renderer_modes(tmp_path):
+    """A reference-schema scene file whose "renderer" object selects the opt-in
+    wide traversal and alias sampling: GpuRenderer renders with both (its
+    passes' mean equals one render of the context in the same modes)."""
+    from radiantium_gb300.config import load_scene_file
+    from tests.test_cpu_config import _scene_file
+    r = load_scene_file(_scene_file(tmp_path, {"type": "path", "max_depth": 5},
+                                    {"type": "gpu_wavefront", "spp": 32, "traversal": "wide",
+                                     "light_sampling": "alias"}))
+    r.Start()
+    r.Wait()
+    assert r.IsSuccess and r.CompletedTaskCount == 16
+    d = Device(0)
+    try:
+        d.set_traversal(N.TRAVERSAL_WIDE)
+        d.set_light_sampling(N.LIGHT_SAMPLING_ALIAS)
+        d.upload(r.scene)
+        assert d.traversal() == N.TRAVERSAL_WIDE
+        want = d.render(r.settings).astype(np.float64)
+    finally:
+        d.close()
+    got = r.RenderTarget.astype(np.float64)
+    assert np.allclose(got, want, rtol=1e-5, atol=1e-6 * float(np.abs(want).max()))
