@@ -510,7 +510,7 @@ DF float Sample1D(const float* pdf, const float* cdf, float integ, int n, float 
  * arithmetic is exact integer arithmetic, so every k lands where the host's
  * count of the table assumes. */
 DF int AliasPick(const int2* tab, int n, float u) {
-    const uint32_t k = (uint32_t)(u * 16777216.0f);
+    const uint32_t k = min((uint32_t)(u * 16777216.0f), 16777215u);   /* u < 1 always; kept in range anyway */
     const uint64_t s = (uint64_t)k * (uint32_t)n;
     const int i = (int)(s >> 24);
     const int2 e = __ldg(tab + i);
