@@ -510,6 +510,15 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, st, args.cpu_seconds,
                            frame_nodes_per_sample=counts["node_visits"] / max(1, counts["samples"]))
+    if relmse is not None:
+        # time to reach this relMSE: every arm computes the same per-sample values,
+        # so each needs the frame's samples, at its own rate
+        frame_samples = samples_step * args.steps
+        relmse["seconds_to_reach"] = {
+            "gpu": args.steps * ms_step / 1000.0,
+            "gpu_e2e": frame_samples * world / e2e["value"] if e2e else None,
+            "plain_megakernel": frame_samples / plain["value"] if plain else None,
+            "cpu": frame_samples / cpu["value"] if cpu else None}
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
