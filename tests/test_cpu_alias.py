@@ -92,6 +92,7 @@ CASES = {
     "single_entry": lambda: np.array([2.0]),
     "heavy_tail_3001": lambda: np.random.default_rng(4).pareto(0.7, 3001),
     "tiny_values_333": lambda: np.random.default_rng(5).random(333) * 1e-30,
+    "wide_row_8191": lambda: _env_row_weights(8191, 4, 6)[2],
 }
 
 
